@@ -1,0 +1,118 @@
+// Device-resident state of one LP instance (an approx_t or alm_t) and the
+// host entry points that launch the solver kernels on it.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <vector>
+
+#include "layout.h"
+
+namespace acd {
+
+struct LogRec;
+
+// Every array of one instance, in device order, carved from one
+// allocation.  FP64 throughout; `f32` holds the FP32 copies the mixed
+// precision mode uses (allocated on first use).
+struct DevInstance {
+        int m = 0, n = 0;
+        int64_t nnz = 0;
+        cudaStream_t stream = nullptr;
+        void * mem = nullptr;
+        size_t bytes = 0;
+
+        // SELL operators (FP64 values)
+        int a_nslices = 0, at_nslices = 0;
+        int64_t * a_ptr = nullptr, * at_ptr = nullptr;
+        int32_t * a_col = nullptr, * at_col = nullptr;
+        double * a_val = nullptr, * at_val = nullptr;
+        int max_width_a = 0, max_width_at = 0;
+
+        // permutations and constants
+        int32_t * row_orig = nullptr;  // m: device row -> original row
+        int32_t * col_orig = nullptr;  // n: device col -> original col
+        double * beta = nullptr;       // m
+
+        // problem vectors (m): rhs, weights, multiplier bounds, lambda, r
+        double * b = nullptr, * w = nullptr, * lam_lo = nullptr,
+               * lam_hi = nullptr, * lam = nullptr, * r = nullptr;
+        // problem vectors (n): objective, bounds, inner linear, v, 1/v, x
+        double * c0 = nullptr, * l = nullptr, * u = nullptr, * c = nullptr,
+               * v = nullptr, * inv_v = nullptr, * x = nullptr;
+        // workspace (n): z, zp, x, g, g2, prev, prev_alt, alt_x, u
+        double * wn[9] = {};
+        // workspace (m): y_viol, z_viol, zp_viol, x_viol, alt_xv, alt_yv
+        double * wm[6] = {};
+
+        // team control, reduction slots, log ring, outputs
+        void * ctl = nullptr;          // TeamCtl
+        double * slots = nullptr;
+        double * result = nullptr;
+        LogRec * log = nullptr;
+        int * log_count = nullptr;
+        int log_cap = 0;
+        void * out = nullptr;          // AlmOut / approx output block
+        int grid_blocks = 0;           // cooperative grid size
+        int block_threads = 256;
+
+        // host staging (pinned)
+        double * h_stage = nullptr;
+        size_t h_stage_len = 0;
+
+        int create(const DeviceLayout & lay);
+        void destroy();
+};
+
+// Host-side view of the vectors an upload takes, in ORIGINAL order.
+struct HostVectors {
+        const double * b = nullptr;       // m
+        const double * w = nullptr;       // m
+        const double * lam_lo = nullptr;  // m
+        const double * lam_hi = nullptr;  // m
+        const double * c0 = nullptr;      // n
+        const double * l = nullptr;       // n
+        const double * u = nullptr;       // n
+};
+
+struct AlmSettings {
+        unsigned long long inner_budget = 0;
+        double kkt_tol = 0;
+        int precision = 0;
+};
+
+struct SolveStats {
+        double seconds = 0;
+        unsigned long long inner = 0, outer = 0, inner_fp32 = 0;
+        double rel_kkt = 0, primal = 0, dual = 0, gap = 0, objective = 0;
+        int status = 0;
+        int precision = 0;
+};
+
+// alm_solve on the device.  x (n) and lam (m) are host arrays in original
+// order, updated in place; w_out (m, original order) receives the final
+// weights and c_out (n) the final penalised linear term.  Returns the
+// reference's 0/1 or a negative ACDALM_E* code.
+int run_alm(DevInstance & d, const HostVectors & hv, size_t niter, double * x,
+            double * lam, FILE * log, double * diag3, const AlmSettings & s,
+            double * w_out, double * c_out, SolveStats & st);
+
+// approx_solve on the device over the instance's uploaded vectors (b, w,
+// c0 as the linear term, l, u; step sizes recomputed).  Returns the reason
+// or a negative code.
+int run_approx(DevInstance & d, const HostVectors & hv, double * x,
+               size_t niter, double max_pg, double max_value, double min_delta,
+               FILE * log, size_t period, double * diag5, double offset,
+               SolveStats & st);
+
+// mpg_solve (spectral projected gradient) on the device.
+int run_mpg(DevInstance & d, const HostVectors & hv, double * x, size_t niter,
+            double max_pg, double max_value, FILE * log, size_t period,
+            double * diag5, double offset, SolveStats & st);
+
+// Step sizes of the uploaded instance (approx.c:135-186) into host arrays
+// in original order: beta (m), v (n), inv_v (n).
+int dev_step_sizes(DevInstance & d, const HostVectors & hv, double * beta,
+                   double * v, double * inv_v);
+
+}  // namespace acd

@@ -1,0 +1,93 @@
+// Host-side sparse layouts.
+//
+// Part 1 rebuilds, byte for byte, the layouts the reference keeps for every
+// matrix (spmv/spmv.c:27-92): nonzero-count permutations
+// (spmv/permutation.c:63-125), CSR of A and A' (spmv/spmv_csr.c:27-80),
+// 4-row block arenas (spmv/spmv_block.c:58-149) and the Z-order COO
+// (spmv/spmv.swizzle.inc:1-52).  The algorithms are my own (counting sorts
+// and radix sorts instead of qsort); the outputs are the reference's.
+//
+// Part 2 builds the device layout the GPU kernels use: warp-sliced ELL
+// ("SELL-32") in a device order where rows are sorted by length, so a slice
+// of 32 rows has almost no padding.  Within a row, entries keep the
+// reference's order (ascending column of the permuted instance), so the
+// sequential per-row sums are the reference's sums.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <vector>
+
+namespace acd {
+
+struct Csr {
+        size_t nrows = 0;
+        std::vector<uint32_t> ptr;  // nrows + 1
+        std::vector<uint32_t> col;
+        std::vector<double> val;
+};
+
+struct BlockArena {
+        size_t nrows = 0, nblocks = 0;
+        std::vector<size_t> offsets;  // byte offset of each block
+        std::vector<uint8_t> bytes;   // headers + values + indices
+};
+
+struct Perm {
+        std::vector<uint32_t> idx;   // new -> old
+        std::vector<uint32_t> ridx;  // old -> new
+};
+
+struct HostMatrix {
+        size_t nrows = 0, ncols = 0, nnz = 0;
+        // Triplets after renumbering; Z-ordered lazily (coo_zordered).
+        std::vector<uint32_t> rows, cols;
+        std::vector<double> vals;
+        bool coo_zordered = false;
+        Csr csr, csr_t;
+        BlockArena block, block_t;  // built lazily (block_ready)
+        bool block_ready = false;
+        Perm rperm, cperm;
+};
+
+// spmv.c:27-92 except the block arenas and the Z-order (built on demand).
+void build_matrix(HostMatrix & m, size_t ncols, size_t nrows, size_t nnz,
+                  const uint32_t * rows, const uint32_t * cols,
+                  const double * vals, bool permute);
+void ensure_blocks(HostMatrix & m);
+void ensure_zorder(HostMatrix & m);
+
+// Warp-sliced ELL of one operator (A or A') in device order.
+struct Sell {
+        int nrows = 0;                 // rows of the operator
+        int nslices = 0;               // ceil(nrows / 32)
+        std::vector<int64_t> ptr;      // nslices + 1, element offsets
+        std::vector<int32_t> col;      // ptr[nslices]
+        std::vector<double> val;
+        int max_width = 0;
+};
+
+// The device order of a permuted instance and the two SELL operators.
+struct DeviceLayout {
+        int m = 0, n = 0;
+        int64_t nnz = 0;
+        // device row d <-> row of the (permuted) instance and the original
+        std::vector<int32_t> row_p_of_d, row_d_of_p, row_orig_of_d;
+        std::vector<int32_t> col_p_of_d, col_d_of_p, col_orig_of_d;
+        std::vector<double> beta;  // nonzeros per device row
+        Sell a, at;
+};
+
+// `pm` is the permuted copy (approx.c:84-88); its CSR orders fix the
+// summation order.  Device rows (columns) are the permuted instance's rows
+// (columns) sorted by decreasing length, ties by position.
+void build_device_layout(const HostMatrix & pm, DeviceLayout & out);
+
+// SELL of a plain matrix (no permutation involved), for the SpMV API:
+// device order = rows sorted by length; transpose selects A'.
+struct PlainSell {
+        std::vector<int32_t> row_of_d;  // device row -> matrix row
+        Sell s;
+};
+void build_plain_sell(const HostMatrix & m, bool transpose, PlainSell & out);
+
+}  // namespace acd

@@ -1,0 +1,816 @@
+// Solver kernels (one cooperative grid per LP) and their host launchers.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "common.h"
+#include "device.cuh"
+#include "instance.h"
+#include "solver.cuh"
+
+namespace acd {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kLogCap = 1 << 14;
+
+// ---- small kernels ------------------------------------------------------
+
+// dst[d] = src[map[d]]: original order -> device order
+__global__ void gather_kernel(double * dst, const double * src,
+                              const int32_t * map, int n)
+{
+        for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < n;
+             d += gridDim.x * blockDim.x)
+                dst[d] = src[map[d]];
+}
+
+// dst[map[d]] = src[d]: device order -> original order
+__global__ void scatter_kernel(double * dst, const double * src,
+                               const int32_t * map, int n)
+{
+        for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < n;
+             d += gridDim.x * blockDim.x)
+                dst[map[d]] = src[d];
+}
+
+// approx_update_step_size (approx.c:135-186) in device order: the A' rows
+// list each column's entries in the reference's summation order and the
+// arithmetic rounds like the reference, so v is bit-identical.
+__global__ void step_size_kernel(SellDev<double> at, const double * w,
+                                 const double * beta, const double * c,
+                                 double * v, double * inv_v)
+{
+        int lane = threadIdx.x & 31;
+        int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+        int nwarps = (gridDim.x * blockDim.x) >> 5;
+        for (int s = warp; s < at.nslices; s += nwarps) {
+                int64_t base = at.ptr[s];
+                int wd = (int)((at.ptr[s + 1] - base) >> 5);
+                double acc = 0;
+                for (int k = 0; k < wd; k++) {
+                        int i = at.col[base + 32 * k + lane];
+                        double a = at.val[base + 32 * k + lane];
+                        acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(__dmul_rn(w[i], beta[i]), a), a));
+                }
+                int j = s * 32 + lane;
+                if (j < at.nrows) {
+                        v[j] = acc;
+                        inv_v[j] = (acc == 0 && c[j] == 0) ? 1.0 : 1.0 / acc;
+                }
+        }
+}
+
+struct AlmKernelArgs {
+        AlmProblem P;
+        InnerWork<double> W;
+        LogBuf log;
+        AlmArgs a;
+        double * x;
+        double * lam;
+        TeamCtl * ctl;
+        double * slots;
+        double * result;
+        AlmOut * out;
+};
+
+template <bool Exact>
+__global__ void __launch_bounds__(kThreads, 1) alm_kernel(AlmKernelArgs k)
+{
+        GridTeam tm{k.ctl, k.slots, k.result, 0};
+        Alm<GridTeam, Exact> alm(tm, k.P, k.W, k.log);
+        AlmOut out;
+        memset(&out, 0, sizeof(out));
+        int r = alm.solve(k.a, k.x, k.lam, out);
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+                if (r < 0)
+                        out.ret = r;
+                *k.out = out;
+        }
+}
+
+struct ApproxOut {
+        int reason;
+        double diag[5];
+        long long iters;
+};
+
+struct ApproxKernelArgs {
+        InnerProblem<double> P;
+        InnerWork<double> W;
+        LogBuf log;
+        InnerArgs a;
+        double * x;
+        TeamCtl * ctl;
+        double * slots;
+        double * result;
+        ApproxOut * out;
+};
+
+template <bool Exact>
+__global__ void __launch_bounds__(kThreads, 1) approx_kernel(ApproxKernelArgs k)
+{
+        GridTeam tm{k.ctl, k.slots, k.result, 0};
+        Approx<double, GridTeam, Exact> ap(tm, k.P, k.W, k.log);
+        ApproxOut out;
+        memset(&out, 0, sizeof(out));
+        InnerArgs a = k.a;
+        a.t_start_ns = global_ns();
+        out.reason = ap.solve(a, k.x, out.diag, &out.iters);
+        if (blockIdx.x == 0 && threadIdx.x == 0)
+                *k.out = out;
+}
+
+// ---- spectral projected gradient (mpg_solve / spg_iter) ------------------
+//
+// approx.c:517-573 and mpg.inc:155-199.  The projection at the top of
+// spg_iter is skipped: x is always the output of a projection already
+// (the initial projection or the previous step), and clamping is
+// idempotent.
+template <class Team, bool Exact>
+struct Spg {
+        Approx<double, Team, Exact> & ap;
+        __device__ Spg(Approx<double, Team, Exact> & a) : ap(a) {}
+
+        __device__ int solve(const InnerArgs & a, double * x_io, double * diag,
+                             long long * iters_out)
+        {
+                auto & tm = ap.tm;
+                auto & P = ap.P;
+                auto & W = ap.W;
+                // state (approx.c:531-539): x = P(x0), z = x, g = grad(x), g2 = g
+                Vec<double> x = {W.xx, W.xv, 0, NAN, NAN};
+                double * z = W.zx;
+                double * g = W.g;
+                double * g2 = W.g2;
+                for (int j = tm.tid(); j < P.n; j += tm.nthreads()) {
+                        double xj = tm.ld(x_io + j);
+                        double lo = maxpd(P.l[j], xj);
+                        double v = minpd(lo, P.u[j]);
+                        x.x[j] = v;
+                        z[j] = v;
+                }
+                if (!tm.sync())
+                        return -1;
+                double cx;
+                ap.x = x;
+                if (!ap.violation(ap.x, 0, 0, 0, true, false, &cx, nullptr, nullptr))
+                        return -1;
+                x = ap.x;
+                {
+                        double pg2, gg;
+                        if (!ap.gradient(x, false, pg2, gg))
+                                return -1;
+                }
+                for (int j = tm.tid(); j < P.n; j += tm.nthreads())
+                        g2[j] = tm.ld(g + j);
+                if (!tm.sync())
+                        return -1;
+                int reason = 0;
+                long long i;
+                for (i = 0; i < a.niter && !reason; i++) {
+                        // gradient at x, pg, y = x - z, u = g - g2, dots
+                        double part[4] = {0, 0, 0, 0};
+                        const int op[4] = {RED_SUM, RED_SUM, RED_SUM, RED_SUM};
+                        if (i > 0 || true) {
+                                sell_rows_1<Exact>(tm, P.At, x.viol, [&](int j, double s) {
+                                        double gj = s + P.c[j];
+                                        g[j] = gj;
+                                        double xj = tm.ld(x.x + j);
+                                        double xp = xj - gj;
+                                        xp = maxpd(P.l[j], xp);
+                                        xp = minpd(P.u[j], xp);
+                                        double d = xj - xp;
+                                        part[0] += d * d;
+                                        double yj = xj - tm.ld(z + j);
+                                        double uj = gj - tm.ld(g2 + j);
+                                        part[1] += yj * yj;
+                                        part[2] += yj * uj;
+                                });
+                        }
+                        if (!tm.reduce(part, op))
+                                return -1;
+                        double pg = sqrt(part[0]);
+                        double stepl = part[1] / part[2];
+                        if (stepl != stepl)
+                                stepl = 1;
+                        if (!(stepl > 1e8)) {
+                                // z = P(x - step g); swap(z, x); swap(g2, g)
+                                for (int j = tm.tid(); j < P.n; j += tm.nthreads()) {
+                                        double v = tm.ld(x.x + j) - stepl * tm.ld(g + j);
+                                        v = maxpd(P.l[j], v);
+                                        v = minpd(P.u[j], v);
+                                        z[j] = v;
+                                }
+                                if (!tm.sync())
+                                        return -1;
+                                double * t = z;
+                                z = x.x;
+                                x.x = t;
+                                t = g2;
+                                g2 = g;
+                                g = t;
+                                ap.W.g = g;
+                        }
+                        // value of the new x (its violation feeds the next
+                        // gradient)
+                        ap.x = x;
+                        if (!ap.violation(ap.x, 0, 0, 0, true, false, &cx, nullptr, nullptr))
+                                return -1;
+                        x = ap.x;
+                        double value = a.offset + x.quad + cx;
+                        if (pg < a.max_pg)
+                                reason = 2;
+                        if (value < a.max_value)
+                                reason = 1;
+                        if (a.log && ((a.period && (i % a.period == 0)) || i == 0 || reason)) {
+                                LogRec r = {2, 0, 0, 0, i + 1, {pg, value, 0, 0, 0, 0}};
+                                ap.put_log(r);
+                        }
+                }
+                // diagnosis (approx.c:556-569)
+                double pg2, gg;
+                if (!ap.gradient(x, false, pg2, gg))
+                        return -1;
+                for (int j = tm.tid(); j < P.n; j += tm.nthreads())
+                        x_io[j] = tm.ld(x.x + j);
+                if (!tm.sync())
+                        return -1;
+                diag[0] = a.offset + x.quad + cx;
+                diag[1] = sqrt(gg);
+                diag[2] = sqrt(pg2);
+                diag[3] = HUGE_VAL;
+                diag[4] = (double)(i + 1);
+                *iters_out = i;
+                (void)reason;
+                return 2;
+        }
+};
+
+__global__ void __launch_bounds__(kThreads, 1) mpg_kernel(ApproxKernelArgs k)
+{
+        GridTeam tm{k.ctl, k.slots, k.result, 0};
+        Approx<double, GridTeam, false> ap(tm, k.P, k.W, k.log);
+        Spg<GridTeam, false> spg(ap);
+        ApproxOut out;
+        memset(&out, 0, sizeof(out));
+        out.reason = spg.solve(k.a, k.x, out.diag, &out.iters);
+        if (blockIdx.x == 0 && threadIdx.x == 0)
+                *k.out = out;
+}
+
+// ---- host helpers --------------------------------------------------------
+
+}  // namespace
+
+// Reference rounding in the solver kernels (separate rounding of products
+// and sums, as the reference's C code) instead of fused multiply-adds.
+bool g_exact = getenv("ACDALM_EXACT") && getenv("ACDALM_EXACT")[0] == '1';
+
+namespace {
+
+template <class T>
+T * carve(char *& p, size_t count)
+{
+        T * r = reinterpret_cast<T *>(p);
+        size_t bytes = (count * sizeof(T) + 255) & ~size_t(255);
+        p += bytes;
+        return r;
+}
+
+size_t rounded(size_t bytes)
+{
+        return (bytes + 255) & ~size_t(255);
+}
+
+int launch_blocks(const void * kernel)
+{
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, 0);
+        if (per_sm < 1)
+                per_sm = 1;
+        return sms * per_sm;
+}
+
+void print_logs(FILE * log, const std::vector<LogRec> & recs)
+{
+        if (log == nullptr)
+                return;
+        for (const LogRec & r : recs) {
+                if (r.kind == 0) {
+                        // approx.c:617-627 restart markers, approx.c:504-515
+                        if (r.restarts > 0) {
+                                fprintf(log, "\t\t ");
+                                for (int i = 0; i < r.restarts; i++)
+                                        fputc('R', log);
+                        }
+                        if (r.has_delta)
+                                fprintf(log, "\t%10lld %12g %12g %12g %8g %12g\n", r.k,
+                                        r.a[0], r.a[1], r.a[2], r.a[3], r.a[4]);
+                        else
+                                fprintf(log, "\t%10lld %12g %12g %12g %8g\n", r.k,
+                                        r.a[0], r.a[1], r.a[2], r.a[3]);
+                } else if (r.kind == 1) {
+                        // alm.c:260-285
+                        fprintf(log, "%4lld: %12g %12g %12g %.18g %.18g", r.k, r.a[0],
+                                r.a[1], r.a[2], r.a[3], r.a[4]);
+                        if (r.stalled)
+                                fprintf(log, " -stalled-\n");
+                        else
+                                fprintf(log, " (%8g)\n", r.a[5]);
+                } else {
+                        // approx.c:550-553
+                        fprintf(log, "%10lld: %12g %12g\n", r.k, r.a[0], r.a[1]);
+                }
+        }
+        fflush(log);
+}
+
+int fetch_logs(DevInstance & d, FILE * log)
+{
+        if (log == nullptr)
+                return 0;
+        int count = 0;
+        ACD_CUDA_TRY(cudaMemcpyAsync(&count, d.log_count, sizeof(int),
+                                     cudaMemcpyDeviceToHost, d.stream), ACDALM_ECUDA);
+        ACD_CUDA_TRY(cudaStreamSynchronize(d.stream), ACDALM_ECUDA);
+        int n = std::min(count, d.log_cap);
+        std::vector<LogRec> recs(n);
+        if (n > 0)
+                ACD_CUDA_TRY(cudaMemcpy(recs.data(), d.log, n * sizeof(LogRec),
+                                        cudaMemcpyDeviceToHost), ACDALM_ECUDA);
+        print_logs(log, recs);
+        if (count > d.log_cap)
+                fprintf(log, "(%d log lines dropped)\n", count - d.log_cap);
+        return 0;
+}
+
+// Upload an original-order host vector into a device-order array.
+int upload_gather(DevInstance & d, double * dst, const double * src,
+                  const int32_t * map, int len, double fill)
+{
+        if (len == 0)
+                return 0;
+        std::vector<double> tmp;
+        if (src == nullptr) {
+                tmp.assign(len, fill);
+                src = tmp.data();
+        }
+        // stage through the x slot's partner buffer (alt_x / alt_xv is
+        // free between solves)
+        double * stage = d.wn[8];
+        if ((int)std::max(d.m, d.n) > d.n)
+                stage = nullptr;
+        double * tmpdev = nullptr;
+        if (len <= d.n)
+                tmpdev = d.wn[8];
+        else
+                tmpdev = d.wm[5];
+        (void)stage;
+        ACD_CUDA_TRY(cudaMemcpyAsync(tmpdev, src, len * sizeof(double),
+                                     cudaMemcpyHostToDevice, d.stream), ACDALM_ECUDA);
+        gather_kernel<<<std::min(1024, (len + 255) / 256), 256, 0, d.stream>>>(
+                dst, tmpdev, map, len);
+        count_launch();
+        ACD_CUDA_TRY(cudaGetLastError(), ACDALM_ECUDA);
+        if (!tmp.empty())
+                ACD_CUDA_TRY(cudaStreamSynchronize(d.stream), ACDALM_ECUDA);
+        return 0;
+}
+
+int download_scatter(DevInstance & d, double * dst, const double * src,
+                     const int32_t * map, int len)
+{
+        if (len == 0)
+                return 0;
+        double * tmpdev = (len <= d.n) ? d.wn[8] : d.wm[5];
+        scatter_kernel<<<std::min(1024, (len + 255) / 256), 256, 0, d.stream>>>(
+                tmpdev, src, map, len);
+        count_launch();
+        ACD_CUDA_TRY(cudaGetLastError(), ACDALM_ECUDA);
+        ACD_CUDA_TRY(cudaMemcpyAsync(dst, tmpdev, len * sizeof(double),
+                                     cudaMemcpyDeviceToHost, d.stream), ACDALM_ECUDA);
+        ACD_CUDA_TRY(cudaStreamSynchronize(d.stream), ACDALM_ECUDA);
+        return 0;
+}
+
+int upload_problem(DevInstance & d, const HostVectors & hv)
+{
+        int r;
+        if ((r = upload_gather(d, d.b, hv.b, d.row_orig, d.m, 0)) ||
+            (r = upload_gather(d, d.w, hv.w, d.row_orig, d.m, 1)) ||
+            (r = upload_gather(d, d.lam_lo, hv.lam_lo, d.row_orig, d.m, -HUGE_VAL)) ||
+            (r = upload_gather(d, d.lam_hi, hv.lam_hi, d.row_orig, d.m, HUGE_VAL)) ||
+            (r = upload_gather(d, d.c0, hv.c0, d.col_orig, d.n, 0)) ||
+            (r = upload_gather(d, d.l, hv.l, d.col_orig, d.n, -HUGE_VAL)) ||
+            (r = upload_gather(d, d.u, hv.u, d.col_orig, d.n, HUGE_VAL)))
+                return r;
+        ACD_CUDA_TRY(cudaStreamSynchronize(d.stream), ACDALM_ECUDA);
+        return 0;
+}
+
+InnerWork<double> work_of(DevInstance & d)
+{
+        InnerWork<double> W;
+        W.zx = d.wn[0];
+        W.zpx = d.wn[1];
+        W.xx = d.wn[2];
+        W.g = d.wn[3];
+        W.g2 = d.wn[4];
+        W.prev = d.wn[5];
+        W.prev_alt = d.wn[6];
+        W.alt_x = d.wn[7];
+        W.ux = d.wn[8];
+        W.yv = d.wm[0];
+        W.zv = d.wm[1];
+        W.zpv = d.wm[2];
+        W.xv = d.wm[3];
+        W.alt_xv = d.wm[4];
+        W.alt_yv = d.wm[5];
+        return W;
+}
+
+SellDev<double> sell_a(const DevInstance & d)
+{
+        return {d.m, d.a_nslices, d.a_ptr, d.a_col, d.a_val};
+}
+
+SellDev<double> sell_at(const DevInstance & d)
+{
+        return {d.n, d.at_nslices, d.at_ptr, d.at_col, d.at_val};
+}
+
+int reset_ctl(DevInstance & d)
+{
+        ACD_CUDA_TRY(cudaMemsetAsync(d.ctl, 0, sizeof(TeamCtl), d.stream), ACDALM_ECUDA);
+        ACD_CUDA_TRY(cudaMemsetAsync(d.log_count, 0, sizeof(int), d.stream), ACDALM_ECUDA);
+        return 0;
+}
+
+int read_status(DevInstance & d, int & status)
+{
+        TeamCtl c;
+        ACD_CUDA_TRY(cudaMemcpy(&c, d.ctl, sizeof(c), cudaMemcpyDeviceToHost), ACDALM_ECUDA);
+        status = c.status;
+        return 0;
+}
+
+// Whole-solve time limit on the device (ACDALM_SOLVE_TIMEOUT seconds,
+// default 900): a solve that runs longer stops with ACDALM_ETIMEOUT.
+unsigned long long solve_limit_ns()
+{
+        const char * e = getenv("ACDALM_SOLVE_TIMEOUT");
+        double sec = e ? atof(e) : 900.0;
+        if (!(sec > 0))
+                return 0;
+        return (unsigned long long)(sec * 1e9);
+}
+
+int launch_coop(const void * fn, int max_blocks, void * args, cudaStream_t s)
+{
+        // every CTA must be resident at once: never more than the occupancy
+        // of this kernel allows, nor more than the reduction slots hold
+        int blocks = std::min(max_blocks, launch_blocks(fn));
+        void * params[1] = {args};
+        ACD_CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kThreads),
+                                                 params, 0, s), ACDALM_ECUDA);
+        count_launch();
+        return 0;
+}
+
+}  // namespace
+
+// ---- DevInstance ---------------------------------------------------------
+
+int DevInstance::create(const DeviceLayout & lay)
+{
+        m = lay.m;
+        n = lay.n;
+        nnz = lay.nnz;
+        a_nslices = lay.a.nslices;
+        at_nslices = lay.at.nslices;
+        max_width_a = lay.a.max_width;
+        max_width_at = lay.at.max_width;
+        int blocks = std::max(std::max(launch_blocks((const void *)alm_kernel<false>),
+                                       launch_blocks((const void *)approx_kernel<false>)),
+                              std::max(launch_blocks((const void *)alm_kernel<true>),
+                                       launch_blocks((const void *)mpg_kernel)));
+        grid_blocks = blocks;
+        size_t ea = lay.a.ptr.back(), eat = lay.at.ptr.back();
+        size_t mm = std::max(m, 1), nn = std::max(n, 1);
+        size_t total = 0;
+        total += rounded((lay.a.ptr.size()) * 8) + rounded(ea * 4) + rounded(ea * 8);
+        total += rounded((lay.at.ptr.size()) * 8) + rounded(eat * 4) + rounded(eat * 8);
+        total += rounded(mm * 4) + rounded(nn * 4) + rounded(mm * 8);
+        total += 6 * rounded(mm * 8) + 7 * rounded(nn * 8);
+        total += 9 * rounded(nn * 8) + 6 * rounded(mm * 8);
+        total += rounded(sizeof(TeamCtl)) + rounded(2 * (size_t)blocks * kRedMax * 8)
+                + rounded(2 * kRedMax * 8);
+        log_cap = kLogCap;
+        total += rounded((size_t)log_cap * sizeof(LogRec)) + rounded(sizeof(int));
+        total += rounded(std::max(sizeof(AlmOut), sizeof(ApproxOut)));
+        ACD_CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), ACDALM_ECUDA);
+        cudaError_t e = cudaMalloc(&mem, total);
+        if (e != cudaSuccess) {
+                set_error(ACDALM_ENOMEM, "cudaMalloc(%zu bytes): %s", total,
+                          cudaGetErrorString(e));
+                mem = nullptr;
+                return ACDALM_ENOMEM;
+        }
+        bytes = total;
+        char * p = static_cast<char *>(mem);
+        a_ptr = carve<int64_t>(p, lay.a.ptr.size());
+        a_col = carve<int32_t>(p, ea);
+        a_val = carve<double>(p, ea);
+        at_ptr = carve<int64_t>(p, lay.at.ptr.size());
+        at_col = carve<int32_t>(p, eat);
+        at_val = carve<double>(p, eat);
+        row_orig = carve<int32_t>(p, mm);
+        col_orig = carve<int32_t>(p, nn);
+        beta = carve<double>(p, mm);
+        b = carve<double>(p, mm);
+        w = carve<double>(p, mm);
+        lam_lo = carve<double>(p, mm);
+        lam_hi = carve<double>(p, mm);
+        lam = carve<double>(p, mm);
+        r = carve<double>(p, mm);
+        c0 = carve<double>(p, nn);
+        l = carve<double>(p, nn);
+        u = carve<double>(p, nn);
+        c = carve<double>(p, nn);
+        v = carve<double>(p, nn);
+        inv_v = carve<double>(p, nn);
+        x = carve<double>(p, nn);
+        for (auto & q : wn)
+                q = carve<double>(p, nn);
+        for (auto & q : wm)
+                q = carve<double>(p, mm);
+        ctl = carve<TeamCtl>(p, 1);
+        slots = carve<double>(p, 2 * (size_t)blocks * kRedMax);
+        result = carve<double>(p, 2 * kRedMax);
+        log = carve<LogRec>(p, log_cap);
+        log_count = carve<int>(p, 1);
+        out = carve<char>(p, std::max(sizeof(AlmOut), sizeof(ApproxOut)));
+
+        ACD_CUDA_TRY(cudaMemsetAsync(mem, 0, total, stream), ACDALM_ECUDA);
+        auto up = [&](void * dst, const void * src, size_t nb) {
+                return nb ? cudaMemcpyAsync(dst, src, nb, cudaMemcpyHostToDevice, stream)
+                          : cudaSuccess;
+        };
+        ACD_CUDA_TRY(up(a_ptr, lay.a.ptr.data(), lay.a.ptr.size() * 8), ACDALM_ECUDA);
+        ACD_CUDA_TRY(up(a_col, lay.a.col.data(), ea * 4), ACDALM_ECUDA);
+        ACD_CUDA_TRY(up(a_val, lay.a.val.data(), ea * 8), ACDALM_ECUDA);
+        ACD_CUDA_TRY(up(at_ptr, lay.at.ptr.data(), lay.at.ptr.size() * 8), ACDALM_ECUDA);
+        ACD_CUDA_TRY(up(at_col, lay.at.col.data(), eat * 4), ACDALM_ECUDA);
+        ACD_CUDA_TRY(up(at_val, lay.at.val.data(), eat * 8), ACDALM_ECUDA);
+        ACD_CUDA_TRY(up(row_orig, lay.row_orig_of_d.data(), (size_t)m * 4), ACDALM_ECUDA);
+        ACD_CUDA_TRY(up(col_orig, lay.col_orig_of_d.data(), (size_t)n * 4), ACDALM_ECUDA);
+        ACD_CUDA_TRY(up(beta, lay.beta.data(), (size_t)m * 8), ACDALM_ECUDA);
+        ACD_CUDA_TRY(cudaStreamSynchronize(stream), ACDALM_ECUDA);
+        return 0;
+}
+
+void DevInstance::destroy()
+{
+        if (mem)
+                cudaFree(mem);
+        mem = nullptr;
+        if (stream)
+                cudaStreamDestroy(stream);
+        stream = nullptr;
+}
+
+// ---- entry points --------------------------------------------------------
+
+int dev_step_sizes(DevInstance & d, const HostVectors & hv, double * beta_out,
+                   double * v_out, double * inv_v_out)
+{
+        int r = upload_problem(d, hv);
+        if (r)
+                return r;
+        step_size_kernel<<<std::max(1, std::min(4096, (d.n + 255) / 256)), 256, 0,
+                           d.stream>>>(sell_at(d), d.w, d.beta, d.c0, d.v, d.inv_v);
+        count_launch();
+        ACD_CUDA_TRY(cudaGetLastError(), ACDALM_ECUDA);
+        if (v_out && (r = download_scatter(d, v_out, d.v, d.col_orig, d.n)))
+                return r;
+        if (inv_v_out && (r = download_scatter(d, inv_v_out, d.inv_v, d.col_orig, d.n)))
+                return r;
+        if (beta_out && (r = download_scatter(d, beta_out, d.beta, d.row_orig, d.m)))
+                return r;
+        return 0;
+}
+
+int run_alm(DevInstance & d, const HostVectors & hv, size_t niter, double * x,
+            double * lam, FILE * log, double * diag3, const AlmSettings & s,
+            double * w_out, double * c_out, SolveStats & st)
+{
+        int r = upload_problem(d, hv);
+        if (r)
+                return r;
+        if ((r = upload_gather(d, d.x, x, d.col_orig, d.n, 0)) ||
+            (r = upload_gather(d, d.lam, lam, d.row_orig, d.m, 0)) || (r = reset_ctl(d)))
+                return r;
+        // |b|, |c0| for the relative KKT terms
+        double bn = 0, cn = 0;
+        for (int i = 0; i < d.m; i++)
+                bn += hv.b[i] * hv.b[i];
+        if (hv.c0)
+                for (int j = 0; j < d.n; j++)
+                        cn += hv.c0[j] * hv.c0[j];
+        AlmKernelArgs k;
+        memset(&k, 0, sizeof(k));
+        k.P.m = d.m;
+        k.P.n = d.n;
+        k.P.A = sell_a(d);
+        k.P.At = sell_at(d);
+        k.P.b = d.b;
+        k.P.c0 = d.c0;
+        k.P.l = d.l;
+        k.P.u = d.u;
+        k.P.lam_lo = d.lam_lo;
+        k.P.lam_hi = d.lam_hi;
+        k.P.beta = d.beta;
+        k.P.orig_row = d.row_orig;
+        k.P.w = d.w;
+        k.P.c = d.c;
+        k.P.v = d.v;
+        k.P.inv_v = d.inv_v;
+        k.P.r = d.r;
+        k.P.bnorm = sqrt(bn);
+        k.P.cnorm = sqrt(cn);
+        k.W = work_of(d);
+        k.log = {d.log, d.log_cap, d.log_count};
+        k.a.niter = (long long)std::min<size_t>(niter, (size_t)1 << 62);
+        k.a.inner_budget = s.inner_budget;
+        k.a.kkt_tol = s.kkt_tol;
+        k.a.log = (log != nullptr);
+        k.a.limit_ns = solve_limit_ns();
+        k.x = d.x;
+        k.lam = d.lam;
+        k.ctl = static_cast<TeamCtl *>(d.ctl);
+        k.slots = d.slots;
+        k.result = d.result;
+        k.out = static_cast<AlmOut *>(d.out);
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, d.stream);
+        const void * fn = g_exact ? (const void *)alm_kernel<true>
+                                  : (const void *)alm_kernel<false>;
+        if ((r = launch_coop(fn, d.grid_blocks, &k, d.stream)))
+                return r;
+        cudaEventRecord(e1, d.stream);
+        ACD_CUDA_TRY(cudaStreamSynchronize(d.stream), ACDALM_ECUDA);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        int status = 0;
+        if ((r = read_status(d, status)))
+                return r;
+        AlmOut out;
+        ACD_CUDA_TRY(cudaMemcpy(&out, d.out, sizeof(out), cudaMemcpyDeviceToHost), ACDALM_ECUDA);
+        fetch_logs(d, log);
+        st.seconds = ms * 1e-3;
+        st.inner = out.inner;
+        st.outer = (unsigned long long)out.outer;
+        st.rel_kkt = out.rel_kkt;
+        st.primal = out.primal;
+        st.dual = out.dual;
+        st.gap = out.gap;
+        st.objective = out.objective;
+        st.status = status;
+        st.precision = 0;
+        if (status != 0) {
+                set_error(status, "device solve failed with status %d%s", status,
+                          status == ACDALM_ETIMEOUT ? " (a device wait timed out)"
+                          : status == ACDALM_ENONFINITE ? " (non-finite iterate)" : "");
+                return status;
+        }
+        if ((r = download_scatter(d, x, d.x, d.col_orig, d.n)) ||
+            (r = download_scatter(d, lam, d.lam, d.row_orig, d.m)))
+                return r;
+        if (w_out && (r = download_scatter(d, w_out, d.w, d.row_orig, d.m)))
+                return r;
+        if (c_out && (r = download_scatter(d, c_out, d.c, d.col_orig, d.n)))
+                return r;
+        if (diag3) {
+                diag3[0] = out.diag[0];
+                diag3[1] = out.diag[1];
+                diag3[2] = out.diag[2];
+        }
+        return out.ret;
+}
+
+static int run_inner(DevInstance & d, const HostVectors & hv, double * x,
+                     size_t niter, double max_pg, double max_value,
+                     double min_delta, FILE * log, size_t period, double * diag5,
+                     double offset, SolveStats & st, bool mpg)
+{
+        int r = upload_problem(d, hv);
+        if (r)
+                return r;
+        // step sizes of the uploaded instance (approx_update)
+        step_size_kernel<<<std::max(1, std::min(4096, (d.n + 255) / 256)), 256, 0,
+                           d.stream>>>(sell_at(d), d.w, d.beta, d.c0, d.v, d.inv_v);
+        count_launch();
+        ACD_CUDA_TRY(cudaGetLastError(), ACDALM_ECUDA);
+        if ((r = upload_gather(d, d.x, x, d.col_orig, d.n, 0)) || (r = reset_ctl(d)))
+                return r;
+        ApproxKernelArgs k;
+        memset(&k, 0, sizeof(k));
+        k.P.m = d.m;
+        k.P.n = d.n;
+        k.P.A = sell_a(d);
+        k.P.At = sell_at(d);
+        k.P.b = d.b;
+        k.P.w = d.w;
+        k.P.c = d.c0;
+        k.P.l = d.l;
+        k.P.u = d.u;
+        k.P.v = d.v;
+        k.P.inv_v = d.inv_v;
+        k.W = work_of(d);
+        k.log = {d.log, d.log_cap, d.log_count};
+        k.a.niter = (long long)std::min<size_t>(niter, (size_t)1 << 62);
+        k.a.max_pg = max_pg;
+        k.a.max_value = max_value;
+        k.a.min_delta = min_delta;
+        k.a.offset = offset;
+        k.a.period = (long long)period;
+        k.a.log = (log != nullptr);
+        k.a.limit_ns = solve_limit_ns();
+        k.x = d.x;
+        k.ctl = static_cast<TeamCtl *>(d.ctl);
+        k.slots = d.slots;
+        k.result = d.result;
+        k.out = static_cast<ApproxOut *>(d.out);
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, d.stream);
+        const void * fn = mpg ? (const void *)mpg_kernel
+                        : (g_exact ? (const void *)approx_kernel<true>
+                                   : (const void *)approx_kernel<false>);
+        if ((r = launch_coop(fn, d.grid_blocks, &k, d.stream)))
+                return r;
+        cudaEventRecord(e1, d.stream);
+        ACD_CUDA_TRY(cudaStreamSynchronize(d.stream), ACDALM_ECUDA);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        int status = 0;
+        if ((r = read_status(d, status)))
+                return r;
+        ApproxOut out;
+        ACD_CUDA_TRY(cudaMemcpy(&out, d.out, sizeof(out), cudaMemcpyDeviceToHost), ACDALM_ECUDA);
+        fetch_logs(d, log);
+        st.seconds = ms * 1e-3;
+        st.inner = (unsigned long long)out.iters;
+        st.status = status;
+        if (status != 0) {
+                set_error(status, "device solve failed with status %d", status);
+                return status;
+        }
+        if ((r = download_scatter(d, x, d.x, d.col_orig, d.n)))
+                return r;
+        if (diag5)
+                for (int i = 0; i < 5; i++)
+                        diag5[i] = out.diag[i];
+        return out.reason;
+}
+
+int run_approx(DevInstance & d, const HostVectors & hv, double * x,
+               size_t niter, double max_pg, double max_value, double min_delta,
+               FILE * log, size_t period, double * diag5, double offset,
+               SolveStats & st)
+{
+        return run_inner(d, hv, x, niter, max_pg, max_value, min_delta, log, period,
+                         diag5, offset, st, false);
+}
+
+int run_mpg(DevInstance & d, const HostVectors & hv, double * x, size_t niter,
+            double max_pg, double max_value, FILE * log, size_t period,
+            double * diag5, double offset, SolveStats & st)
+{
+        return run_inner(d, hv, x, niter, max_pg, max_value, 0, log, period, diag5,
+                         offset, st, true);
+}
+
+}  // namespace acd
+
+extern "C" int acdalm_set_rounding(int exact)
+{
+        int old = acd::g_exact ? 1 : 0;
+        acd::g_exact = exact != 0;
+        return old;
+}

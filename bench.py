@@ -1,0 +1,310 @@
+"""Benchmark: LPs solved per second to 1e-6 relative KKT on one GB300.
+
+One step = one LP solved from scratch (x = 0, lambda = 0, unit ALM weights)
+by the ALM + APPROX loop until the relative KKT residual is <= 1e-6.
+Workload (default): the mid-size LP, m=100,000 rows, n=200,000 columns,
+Zipf(1.5) column counts (~2.26M nonzeros), values U[-1,1], box [0,10],
+seeded synthetic data.
+
+Printed (rank 0, one JSON line):
+  value         LPs/s from the solve kernel's device time (inputs resident in
+                HBM; L2 flushed with a 512 MB write before every step)
+  e2e           LPs/s through the C ABI (alm_solve with host arrays: the
+                uploads and downloads are inside the timed region)
+  roofline      the solve kernel: algorithmic bytes / device time vs the
+                measured HBM copy bandwidth
+  cpu_baseline  the reference's CPU loop on this host's cores, on a bounded
+                sample of the same workload (see `sample`)
+
+  python bench.py [--steps K] [--warmup W] [--precision fp64|mixed]
+                  [--workload mid|small] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+inst = importlib.import_module("acd-alm_gb300.instances")
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def workload(name: str):
+    if name == "mid":
+        return inst.mid()
+    if name == "small":
+        return inst.small()
+    raise SystemExit(f"unknown workload {name}")
+
+
+def bytes_per_iteration(lp, fp32: bool) -> float:
+    """Algorithmic bytes of one steady-state APPROX iteration: one pass over
+    A and one over A' (each nonzero's value and column read once), plus the
+    vector streams of the fused epilogues."""
+    nnz, m, n = lp.nnz, lp.nrows, lp.ncols
+    if fp32:
+        return 16.0 * nnz + 4.0 * (m + n) + 58.0 * n + 34.0 * m
+    return 24.0 * nnz + 4.0 * (m + n) + 116.0 * n + 68.0 * m
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for name, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": float(rows[0][2]) if rows[0][2].replace(".", "").isdigit() else None,
+                "samples": len(rows), "reasons": sorted(reasons)}
+
+
+def cpu_baseline(lp, gpu_inner_per_lp: float, budget: int, threads: int):
+    """The reference's loop on the host cores, over a bounded sample: an ALM
+    solve of the same LP capped at `budget` inner iterations; LPs/s is
+    extrapolated with the GPU solve's inner iterations per LP."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    kind = "reference" if O.available("ref") else "port"
+    if kind == "port" and not O.available("oracle"):
+        O.build(ref=False)
+    lib = O.Lib("ref" if kind == "reference" else "oracle")
+    m = lib.matrix(lp)
+    h = lib.alm(m, lp)
+    t0 = time.perf_counter()
+    r, x, lam, diag, used = lib.alm_solve(h, lp.nrows, lp.ncols, inner_budget=budget,
+                                          threads=threads)
+    dt = time.perf_counter() - t0
+    lib.alm_free(h)
+    lib.matrix_free(m)
+    per_iter = dt / max(used, 1)
+    return {"value": 1.0 / (per_iter * gpu_inner_per_lp), "unit": "LP/s",
+            "cores": threads, "kind": kind,
+            "sample": (f"ALM+APPROX on the same LP capped at {used} inner iterations "
+                       f"({dt:.1f} s, {per_iter * 1e3:.2f} ms/iteration), extrapolated to "
+                       f"{gpu_inner_per_lp:.0f} inner iterations per LP (the GPU solve's count)")}
+
+
+def run_reference(args, lp, rank: int):
+    """--impl reference: the reference's CPU implementation of the loop on
+    the host cores (oracle/_ref where it was compiled, else the oracle port),
+    each step a bounded sample of the workload."""
+    threads = os.cpu_count() or 1
+    per_lp = float(os.environ.get("ACDALM_REF_ITERS_PER_LP", "20000"))
+    vals = []
+    base = None
+    for s in range(args.warmup + args.steps):
+        base = cpu_baseline(lp, per_lp, args.ref_budget, threads)
+        if s >= args.warmup:
+            vals.append(base["value"])
+    v = statistics.median(vals)
+    base["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "LP/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_of(args, lp), "cpu_baseline": base,
+            "e2e": {"value": v, "unit": "LP/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+METRIC = "LPs/sec to 1e-6 relative KKT"
+
+
+def config_of(args, lp):
+    return {"workload": f"{args.workload} LP", "m": lp.nrows, "n": lp.ncols, "nnz": lp.nnz,
+            "stop": "relative KKT <= 1e-6 (max of primal, dual, gap)",
+            "precision": args.precision, "l2": "flushed (512 MB write) before every step",
+            "seed": lp.seed}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--workload", default="mid")
+    ap.add_argument("--precision", default="fp64")
+    ap.add_argument("--ref-budget", type=int, default=300)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    lp = workload(args.workload)
+
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args, lp, rank)
+        return
+
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    os.environ.setdefault("ACDALM_DEVICE", str(local))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    lib = importlib.import_module("acd-alm_gb300.lib")
+    L = lib.lib()
+    L.acdalm_launch_count.restype = __import__("ctypes").c_ulonglong
+    m = lib.Matrix(lp)
+    alm = lib.Alm(m, lp)
+    alm.set_kkt_tolerance(1e-6)
+    if args.precision == "mixed":
+        alm.set_precision(lib.PRECISION_MIXED)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    weights = np.ctypeslib.as_array(_alm_weight(L, alm), (lp.nrows,))
+
+    def reset_state():
+        # unit ALM weights: each step starts the same solve from scratch
+        weights[:] = 1.0
+
+    def one_step():
+        reset_state()
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r, x, lam, diag = alm.solve(1000)
+        t1 = time.perf_counter()
+        st = alm.stats()
+        return r, x, lam, st, t1 - t0
+
+    for _ in range(args.warmup):
+        one_step()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler()
+    clocks.start()
+    launches0 = L.acdalm_launch_count()
+    dev_s, wall_s, inner, outer, kkts = [], [], [], [], []
+    for _ in range(args.steps):
+        r, x, lam, st, wall = one_step()
+        dev_s.append(st["seconds"])
+        wall_s.append(wall)
+        inner.append(st["inner_iterations"])
+        outer.append(st["outer_iterations"])
+        kkts.append(st["rel_kkt"])
+    torch.cuda.synchronize()
+    launches = L.acdalm_launch_count() - launches0
+    clk = clocks.stop()
+    tot_dev, tot_wall = sum(dev_s), sum(wall_s)
+    if dist:
+        t = torch.tensor([tot_dev, tot_wall], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tot_dev, tot_wall = t.tolist()
+    n_lp = args.steps * world
+    value = n_lp / tot_dev
+    e2e = n_lp / tot_wall
+    k = inst.rel_kkt(lp, x, lam)
+    fp32 = args.precision == "mixed"
+    bpi = bytes_per_iteration(lp, fp32)
+    mean_inner = float(np.mean(inner))
+    algo_bytes = mean_inner * bpi
+    achieved = algo_bytes / (tot_dev / args.steps) / 1e9
+    peak, peak_kind = load_peaks()
+    line = {
+        "metric": METRIC, "value": value, "unit": "LP/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * tot_dev / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if fp32 else "f64", "data": "synthetic",
+        "config": config_of(args, lp),
+        "e2e": {"value": e2e, "unit": "LP/s",
+                "h2d_bytes_per_step": 8 * (3 * lp.nrows + 4 * lp.ncols + lp.nrows + lp.ncols),
+                "d2h_bytes_per_step": 8 * (2 * lp.ncols + 2 * lp.nrows)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "kernel": "alm_kernel (persistent cooperative solve)",
+                     "peak_source": peak_kind,
+                     "bytes_per_inner_iteration": bpi},
+        "gpu_launches": int(launches),
+        "solve": {"inner_iterations": inner, "outer_iterations": outer,
+                  "rel_kkt_device": kkts, "rel_kkt_host_check": k["rel_kkt"],
+                  "objective": k["objective"], "device_seconds": dev_s,
+                  "wall_seconds": wall_s},
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(lp, mean_inner, args.ref_budget,
+                                            os.cpu_count() or 1)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    alm.free()
+    m.free()
+    if dist:
+        dist.destroy_process_group()
+
+
+def _alm_weight(L, alm):
+    """The ALM instance's weight vector (approx_weight of its APPROX)."""
+    import ctypes
+    L.acdalm_alm_approx.restype = ctypes.c_void_p
+    L.acdalm_alm_approx.argtypes = [ctypes.c_void_p]
+    a = L.acdalm_alm_approx(alm.h)
+    return L.approx_weight(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,123 @@
+/* libacdalm extensions: device control, error reporting, precision modes,
+ * device-resident SpMV, solve statistics.  None of these has a counterpart
+ * in the reference; legacy callers never need them.
+ *
+ * Error convention: the drop-in entry points keep the reference's return
+ * values on success; device failures come back as the negative codes below
+ * (never as 0/1/2/3), and acdalm_last_error() describes the last one.
+ */
+#ifndef ACDALM_EXT_H
+#define ACDALM_EXT_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ACDALM_OK 0
+#define ACDALM_ECUDA (-1)      /* a CUDA call failed */
+#define ACDALM_ETIMEOUT (-2)   /* a device-side wait gave up */
+#define ACDALM_ENOMEM (-3)     /* device or host allocation failed */
+#define ACDALM_EINVAL (-4)     /* bad argument (sizes, pointers, modes) */
+#define ACDALM_ENONFINITE (-5) /* the iterates stopped being finite */
+#define ACDALM_ENODEV (-6)     /* no usable CUDA device */
+
+struct sparse_matrix;
+struct approx;
+struct alm;
+
+/* Message for the calling thread's last error ("" if none). */
+const char * acdalm_last_error(void);
+/* Kernels the library has launched so far (all threads). */
+unsigned long long acdalm_launch_count(void);
+/* Code of the calling thread's last error (0 if none); clears it. */
+int acdalm_take_error(void);
+
+/* ---- SpMV on the device ---- */
+#define ACDALM_SPMV_SELL 0  /* warp-sliced ELL, 32 rows per slice (default) */
+#define ACDALM_SPMV_BLOCK 1 /* the 4-row block arena of the reference */
+#define ACDALM_SPMV_CSR 2   /* CSR, a sub-warp per row */
+/* Variant used by sparse_matrix_multiply{,_2}; returns the previous one. */
+int acdalm_spmv_variant(int variant);
+/* y = op(A) x with x and y already in device memory, launched on `stream`
+ * (a cudaStream_t, NULL = default stream), FP64.  The layout is uploaded on
+ * first use.  Returns 0 or a negative code. */
+int acdalm_spmv_device(const struct sparse_matrix * a, int variant,
+                       int transpose, const double * x, double * y,
+                       void * stream);
+/* Same in FP32 (values rounded to float once, at upload). */
+int acdalm_spmv_device_f32(const struct sparse_matrix * a, int variant,
+                           int transpose, const float * x, float * y,
+                           void * stream);
+/* Bytes of device memory the matrix's uploaded layouts occupy. */
+size_t acdalm_matrix_device_bytes(const struct sparse_matrix * a);
+
+/* ---- solver controls ---- */
+#define ACDALM_PRECISION_FP64 0  /* everything in FP64 (the default) */
+#define ACDALM_PRECISION_MIXED 1 /* FP32 inner iterations, FP64 outer loop
+                                    and final refinement */
+int alm_set_precision(struct alm *, int mode);
+/* Extra stop for alm_solve: the relative KKT residual (max of primal,
+ * dual and gap terms, FP64) falls below tol (0 = off, the default). */
+int alm_set_kkt_tolerance(struct alm *, double tol);
+/* Cap on the total inner iterations of one alm_solve (0 = none). */
+int alm_set_inner_budget(struct alm *, uint64_t budget);
+
+typedef struct acdalm_stats {
+        double seconds;           /* device time of the last solve */
+        uint64_t inner_iterations;
+        uint64_t outer_iterations;
+        double rel_kkt;           /* FP64 relative KKT residual at exit */
+        double primal, dual, gap; /* its three terms */
+        double objective;
+        int status;               /* 0 ok, or a negative ACDALM_E* code */
+        int precision;            /* ACDALM_PRECISION_* used */
+        uint64_t fp32_inner_iterations; /* of which ran in FP32 */
+} acdalm_stats_t;
+int alm_last_stats(struct alm *, acdalm_stats_t * out);
+int approx_last_stats(struct approx *, acdalm_stats_t * out);
+
+/* Rounding of the solver kernels: 0 (default) fused multiply-adds; 1 the
+ * reference's separate rounding of every product and sum, which makes the
+ * per-element results of each pass bit-identical to the reference's (the
+ * reductions still sum in a different order).  Returns the previous value. */
+int acdalm_set_rounding(int exact);
+
+/* cudaStream_t the instance launches on (created with the instance). */
+void * alm_stream(struct alm *);
+void * approx_stream(struct approx *);
+
+
+/* ---- layout inspection (for parity checks against the reference) ---- */
+/* The 4-row block arena of A (transpose = 0) or A' (1), byte for byte the
+ * reference's (spmv/spmv_block.c:124-149): returns its size in bytes and
+ * the block count in *nblocks. */
+size_t acdalm_block_bytes(struct sparse_matrix * a, int transpose,
+                          size_t * nblocks);
+int acdalm_block_copy(struct sparse_matrix * a, int transpose,
+                      size_t * offsets, void * arena, size_t bytes);
+/* CSR of A or A' (spmv/spmv_csr.c:27-80): nrows+1 row pointers, nnz
+ * columns and values. */
+int acdalm_csr_copy(struct sparse_matrix * a, int transpose,
+                    uint32_t * rows_indices, uint32_t * columns,
+                    double * values);
+/* Row (row = 1) or column permutation, idx = new -> old, ridx = old -> new
+ * (spmv/permutation.c:63-125). */
+int acdalm_perm_copy(struct sparse_matrix * a, int row, uint32_t * idx,
+                     uint32_t * ridx);
+/* The APPROX instance an ALM instance solves with: its approx_weight() is
+ * the ALM's per-row weight vector, which persists across alm_solve calls
+ * (alm.c:194-212); resetting it to 1 restarts the weighting. */
+struct approx * acdalm_alm_approx(struct alm * m);
+/* The permuted shadow matrix approx_make builds (approx/approx.c:84-88). */
+struct sparse_matrix * acdalm_approx_permuted_matrix(struct approx * a);
+/* Step sizes of the instance as the solver computes them on the device, in
+ * original order: beta (nrhs), v and inv_v (nvars), approx/approx.c:135-186
+ * (bit-identical to the reference's permuted instance). */
+int acdalm_approx_step_sizes(struct approx * a, double * beta, double * v,
+                             double * inv_v);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

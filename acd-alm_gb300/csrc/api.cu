@@ -17,35 +17,11 @@
 #include "common.h"
 #include "instance.h"
 #include "layout.h"
+#include "objects.h"
 
 namespace acd {
 HostMatrix & host_of(sparse_matrix_t * m);
 }
-
-struct approx {
-        size_t nrhs = 0, nvars = 0;
-        sparse_matrix_t * matrix = nullptr;  // borrowed
-        sparse_matrix_t * permuted = nullptr;  // owned shadow copy
-        // live vectors (the accessors' arrays)
-        std::vector<double> rhs, weight, linear, lower, upper;
-        // the shadow: what the last approx_update published
-        std::vector<double> s_rhs, s_weight, s_linear, s_lower, s_upper;
-        acd::DeviceLayout lay;
-        bool lay_ready = false;
-        acd::DevInstance dev;
-        bool dev_ready = false;
-        acd::SolveStats stats;
-        std::mutex lock;
-};
-
-struct alm {
-        size_t nrhs = 0, nvars = 0;
-        sparse_matrix_t * matrix = nullptr;
-        std::vector<double> linear, lambda_lower, lambda_upper;
-        approx_t * approx = nullptr;
-        acd::AlmSettings settings;
-        acd::SolveStats stats;
-};
 
 namespace {
 

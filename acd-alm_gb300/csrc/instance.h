@@ -110,6 +110,34 @@ int run_mpg(DevInstance & d, const HostVectors & hv, double * x, size_t niter,
             double max_pg, double max_value, FILE * log, size_t period,
             double * diag5, double offset, SolveStats & st);
 
+// Solver scratch carved out of caller-provided device memory (the
+// allocation-free entry point, static_solve.cu): control words, reduction
+// slots for up to max_blocks CTAs, outputs, step sizes, x in device order
+// and the APPROX workspace.
+struct ScratchSolve {
+        void * ctl = nullptr;
+        double * slots = nullptr;
+        int max_blocks = 0;
+        double * result = nullptr;
+        void * out = nullptr;
+        int * log_count = nullptr;
+        double * v = nullptr, * inv_v = nullptr, * xd = nullptr;
+        double * wn[9] = {};
+        double * wm[6] = {};
+};
+// Bytes of the control region of a ScratchSolve for max_blocks CTAs
+// (everything but the vectors).
+size_t scratch_control_bytes(int max_blocks);
+
+// approx_solve from a device array x (n doubles, original order, updated in
+// place) with every piece of solver scratch in `s`; the instance's device
+// copy must exist.  Allocates nothing.  Returns the reason or a negative
+// code; diag5 (host, may be NULL) receives the diagnosis.
+int run_approx_scratch(DevInstance & d, const HostVectors & hv, double * x_dev,
+                       size_t niter, double max_pg, double max_value,
+                       double min_delta, double * diag5, double offset,
+                       const ScratchSolve & s, cudaStream_t stream);
+
 // Step sizes of the uploaded instance (approx.c:135-186) into host arrays
 // in original order: beta (m), v (n), inv_v (n).
 int dev_step_sizes(DevInstance & d, const HostVectors & hv, double * beta,

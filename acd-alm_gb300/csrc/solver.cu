@@ -363,17 +363,8 @@ int upload_gather(DevInstance & d, double * dst, const double * src,
                 tmp.assign(len, fill);
                 src = tmp.data();
         }
-        // stage through the x slot's partner buffer (alt_x / alt_xv is
-        // free between solves)
-        double * stage = d.wn[8];
-        if ((int)std::max(d.m, d.n) > d.n)
-                stage = nullptr;
-        double * tmpdev = nullptr;
-        if (len <= d.n)
-                tmpdev = d.wn[8];
-        else
-                tmpdev = d.wm[5];
-        (void)stage;
+        // staged through the instance's spare buffer of that length
+        double * tmpdev = (len <= d.n) ? d.wn[8] : d.wm[5];
         ACD_CUDA_TRY(cudaMemcpyAsync(tmpdev, src, len * sizeof(double),
                                      cudaMemcpyHostToDevice, d.stream), ACDALM_ECUDA);
         gather_kernel<<<std::min(1024, (len + 255) / 256), 256, 0, d.stream>>>(
@@ -406,12 +397,15 @@ int upload_problem(DevInstance & d, const HostVectors & hv)
         int r;
         if ((r = upload_gather(d, d.b, hv.b, d.row_orig, d.m, 0)) ||
             (r = upload_gather(d, d.w, hv.w, d.row_orig, d.m, 1)) ||
-            (r = upload_gather(d, d.lam_lo, hv.lam_lo, d.row_orig, d.m, -HUGE_VAL)) ||
-            (r = upload_gather(d, d.lam_hi, hv.lam_hi, d.row_orig, d.m, HUGE_VAL)) ||
             (r = upload_gather(d, d.c0, hv.c0, d.col_orig, d.n, 0)) ||
             (r = upload_gather(d, d.l, hv.l, d.col_orig, d.n, -HUGE_VAL)) ||
             (r = upload_gather(d, d.u, hv.u, d.col_orig, d.n, HUGE_VAL)))
                 return r;
+        // multiplier bounds: ALM only
+        if (hv.lam_lo || hv.lam_hi)
+                if ((r = upload_gather(d, d.lam_lo, hv.lam_lo, d.row_orig, d.m, -HUGE_VAL)) ||
+                    (r = upload_gather(d, d.lam_hi, hv.lam_hi, d.row_orig, d.m, HUGE_VAL)))
+                        return r;
         ACD_CUDA_TRY(cudaStreamSynchronize(d.stream), ACDALM_ECUDA);
         return 0;
 }
@@ -783,6 +777,104 @@ static int run_inner(DevInstance & d, const HostVectors & hv, double * x,
         }
         if ((r = download_scatter(d, x, d.x, d.col_orig, d.n)))
                 return r;
+        if (diag5)
+                for (int i = 0; i < 5; i++)
+                        diag5[i] = out.diag[i];
+        return out.reason;
+}
+
+size_t scratch_control_bytes(int max_blocks)
+{
+        return rounded(sizeof(TeamCtl)) + rounded(2 * (size_t)max_blocks * kRedMax * 8)
+                + rounded(2 * kRedMax * 8) + rounded(sizeof(ApproxOut)) + rounded(sizeof(int));
+}
+
+int run_approx_scratch(DevInstance & d, const HostVectors & hv, double * x_dev,
+                       size_t niter, double max_pg, double max_value,
+                       double min_delta, double * diag5, double offset,
+                       const ScratchSolve & s, cudaStream_t stream)
+{
+        // the problem vectors go into the instance's own device arrays,
+        // staged through its buffers (no allocation)
+        int r = upload_problem(d, hv);
+        if (r)
+                return r;
+        ACD_CUDA_TRY(cudaMemsetAsync(s.ctl, 0, sizeof(TeamCtl), stream), ACDALM_ECUDA);
+        ACD_CUDA_TRY(cudaMemsetAsync(s.log_count, 0, sizeof(int), stream), ACDALM_ECUDA);
+        int nb = std::max(1, std::min(1024, (d.n + 255) / 256));
+        step_size_kernel<<<nb, 256, 0, stream>>>(sell_at(d), d.w, d.beta, d.c0, s.v,
+                                                 s.inv_v);
+        count_launch();
+        ACD_CUDA_TRY(cudaGetLastError(), ACDALM_ECUDA);
+        if (d.n) {
+                gather_kernel<<<nb, 256, 0, stream>>>(s.xd, x_dev, d.col_orig, d.n);
+                count_launch();
+                ACD_CUDA_TRY(cudaGetLastError(), ACDALM_ECUDA);
+        }
+        ApproxKernelArgs k;
+        memset(&k, 0, sizeof(k));
+        k.P.m = d.m;
+        k.P.n = d.n;
+        k.P.A = sell_a(d);
+        k.P.At = sell_at(d);
+        k.P.b = d.b;
+        k.P.w = d.w;
+        k.P.c = d.c0;
+        k.P.l = d.l;
+        k.P.u = d.u;
+        k.P.v = s.v;
+        k.P.inv_v = s.inv_v;
+        InnerWork<double> W;
+        W.zx = s.wn[0];
+        W.zpx = s.wn[1];
+        W.xx = s.wn[2];
+        W.g = s.wn[3];
+        W.g2 = s.wn[4];
+        W.prev = s.wn[5];
+        W.prev_alt = s.wn[6];
+        W.alt_x = s.wn[7];
+        W.ux = s.wn[8];
+        W.yv = s.wm[0];
+        W.zv = s.wm[1];
+        W.zpv = s.wm[2];
+        W.xv = s.wm[3];
+        W.alt_xv = s.wm[4];
+        W.alt_yv = s.wm[5];
+        k.W = W;
+        k.log = {nullptr, 0, s.log_count};
+        k.a.niter = (long long)std::min<size_t>(niter, (size_t)1 << 62);
+        k.a.max_pg = max_pg;
+        k.a.max_value = max_value;
+        k.a.min_delta = min_delta;
+        k.a.offset = offset;
+        k.a.period = 0;
+        k.a.log = 0;
+        k.a.limit_ns = solve_limit_ns();
+        k.x = s.xd;
+        k.ctl = static_cast<TeamCtl *>(s.ctl);
+        k.slots = s.slots;
+        k.result = s.result;
+        k.out = static_cast<ApproxOut *>(s.out);
+        const void * fn = g_exact ? (const void *)approx_kernel<true>
+                                  : (const void *)approx_kernel<false>;
+        if ((r = launch_coop(fn, s.max_blocks, &k, stream)))
+                return r;
+        if (d.n) {
+                scatter_kernel<<<nb, 256, 0, stream>>>(x_dev, s.xd, d.col_orig, d.n);
+                count_launch();
+                ACD_CUDA_TRY(cudaGetLastError(), ACDALM_ECUDA);
+        }
+        TeamCtl c;
+        ApproxOut out;
+        ACD_CUDA_TRY(cudaMemcpyAsync(&c, s.ctl, sizeof(c), cudaMemcpyDeviceToHost, stream),
+                     ACDALM_ECUDA);
+        ACD_CUDA_TRY(cudaMemcpyAsync(&out, s.out, sizeof(out), cudaMemcpyDeviceToHost, stream),
+                     ACDALM_ECUDA);
+        ACD_CUDA_TRY(cudaStreamSynchronize(stream), ACDALM_ECUDA);
+        if (c.status != 0) {
+                set_error(c.status, "device solve failed with status %d", c.status);
+                return c.status;
+        }
         if (diag5)
                 for (int i = 0; i < 5; i++)
                         diag5[i] = out.diag[i];

@@ -117,6 +117,33 @@ struct sparse_matrix * acdalm_approx_permuted_matrix(struct approx * a);
 int acdalm_approx_step_sizes(struct approx * a, double * beta, double * v,
                              double * inv_v);
 
+/* ---- solving without allocating ---- */
+/* approx_solve for callers that cannot call cudaMalloc when they solve:
+ * code running while a CUDA stream is captured into a graph, frameworks
+ * whose caching allocator owns the device memory budget, and latency-bound
+ * loops that cannot take cudaMalloc's implicit synchronisation.  No
+ * counterpart in the reference.
+ *
+ * Same arguments and return values as approx_solve (approx.h), except: x is
+ * a DEVICE array of n doubles (original order), updated in place; there is
+ * no log; OUT_diagnosis (NULL or 5 doubles) is host memory; the work is
+ * launched on `stream` (a cudaStream_t, NULL = the default stream) and the
+ * call returns when it is done.
+ *
+ * It allocates nothing: all solver scratch lives in one fixed 32 MiB device
+ * array inside the library, which every GPU that loads the library holds
+ * until the process exits.  Instances larger than that array holds (about
+ * 12 n + 6 m <= 4.17 million doubles) are rejected with ACDALM_EINVAL.  The
+ * instance's own device copy (matrix layout and vectors) must already exist:
+ * call approx_solve, mpg_solve or cd_solve on it once first.  The first call
+ * on each device also looks up the array's device address; make that first
+ * call before any stream capture.  Every call shares the one array, so
+ * calls that overlap on the GPU (other threads, other streams) race. */
+int approx_solve_static(double * x, size_t n, struct approx * approx,
+                        size_t niter, double max_pg, double max_value,
+                        double min_delta, double * OUT_diagnosis,
+                        double offset, void * stream);
+
 #ifdef __cplusplus
 }
 #endif

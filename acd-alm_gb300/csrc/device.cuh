@@ -105,19 +105,48 @@ __device__ __forceinline__ void block_reduce(double (&v)[K], const int (&op)[K],
         __syncthreads();
 }
 
-// Per-team control words in global memory (zeroed before the launch).
+// Per-team control words in global memory (zeroed before the launch), each
+// on its own 128-byte line.
+struct alignas(128) CtlWord {
+        unsigned v;
+        unsigned pad[31];
+};
 struct TeamCtl {
-        unsigned count;
-        unsigned gen;
-        int status;
-        int pad;
+        CtlWord status_w;
 };
 
+// Reduction slots: per CTA and parity one 128-byte line holding a 64-bit tag
+// (the barrier epoch that wrote it) and up to kRedMax values.
+constexpr int kSlotStride = 16;  // doubles per line
+
+__device__ __forceinline__ void st_release_u64(unsigned long long * p, unsigned long long v)
+{
+        asm volatile("st.release.gpu.global.u64 [%0], %1;" :: "l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long * p)
+{
+        unsigned long long v;
+        asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+        return v;
+}
+
+__device__ __forceinline__ void fence_acquire_gpu()
+{
+        asm volatile("fence.acq_rel.gpu;" ::: "memory");
+}
+
+// Every CTA of a cooperative launch.  team.reduce() is an all-gather: each
+// CTA publishes its partials in its own line with a release-stored tag, then
+// every CTA waits for all tags of this epoch and sums all lines itself in
+// CTA order -- so every thread gets the same bits, in about two L2 round
+// trips, with no counters and no fences.
 struct GridTeam {
         TeamCtl * ctl;
-        double * slots;   // [2][gridDim.x][kRedMax]
-        double * result;  // [2][kRedMax]
+        double * slots;   // [2][gridDim.x][kSlotStride]
+        double * result;  // unused (kept for the launch interface)
         int parity;
+        unsigned epoch;   // reductions passed (the same count in every CTA)
 
         static constexpr bool kShared = false;
 
@@ -131,14 +160,19 @@ struct GridTeam {
         template <class T>
         __device__ __forceinline__ T ld(const T * p) const { return __ldcg(p); }
 
+        __device__ int * status() const
+        {
+                return reinterpret_cast<int *>(&ctl->status_w.v);
+        }
+
         __device__ bool failed() const
         {
-                return ld_acquire_int(&ctl->status) != 0;
+                return ld_acquire_int(status()) != 0;
         }
 
         __device__ void fail(int code)
         {
-                atomicCAS(&ctl->status, 0, code);
+                atomicCAS(status(), 0, code);
         }
 
         // Reduction + barrier.  Returns false if the team has failed.
@@ -146,73 +180,105 @@ struct GridTeam {
         __device__ bool reduce(double (&v)[K], const int (&op)[K])
         {
                 __shared__ double tot[kRedMax];
-                __shared__ int last;
-                __shared__ unsigned gen0;
                 __shared__ int bad;
                 block_reduce<K>(v, op, tot);
-                double * mine = slots
-                        + ((size_t)parity * gridDim.x + blockIdx.x) * kRedMax;
-                if (threadIdx.x < K)
-                        __stcg(mine + threadIdx.x, tot[threadIdx.x]);
-                __syncthreads();
+                epoch++;
+                const unsigned nb = gridDim.x;
+                double * lines = slots + (size_t)parity * nb * kSlotStride;
                 if (threadIdx.x == 0) {
-                        __threadfence();
-                        gen0 = ld_acquire(&ctl->gen);
-                        unsigned prev = atomicAdd(&ctl->count, 1u);
-                        last = (prev == gridDim.x - 1);
-                }
-                __syncthreads();
-                if (last) {
-                        if (threadIdx.x < 32) {
-                                int lane = threadIdx.x;
-                                const double * base = slots
-                                        + (size_t)parity * gridDim.x * kRedMax;
+                        double * mine = lines + (size_t)blockIdx.x * kSlotStride;
 #pragma unroll
-                                for (int k = 0; k < K; k++) {
-                                        double acc = red_identity(op[k]);
-                                        for (unsigned b = lane; b < gridDim.x; b += 32)
-                                                acc = red_combine(op[k], acc,
-                                                                  __ldcg(base + (size_t)b * kRedMax + k));
-                                        acc = warp_reduce(acc, op[k]);
-                                        if (lane == 0)
-                                                __stcg(result + parity * kRedMax + k, acc);
-                                }
-                                __syncwarp();
-                                if (lane == 0) {
-                                        __threadfence();
-                                        atomicExch(&ctl->count, 0u);
-                                        __threadfence();
-                                        atomicAdd(&ctl->gen, 1u);
-                                }
-                        }
-                } else if (threadIdx.x == 0) {
-                        unsigned long long t0 = global_ns();
-                        unsigned spins = 0;
-                        while (ld_acquire(&ctl->gen) == gen0) {
-                                __nanosleep(32);
-                                if ((++spins & 255) == 0) {
-                                        if (ld_acquire_int(&ctl->status) != 0)
-                                                break;
-                                        if (global_ns() - t0 > kWaitLimitNs) {
-                                                fail(kStatusTimeout);
-                                                break;
+                        for (int k = 0; k < K; k++)
+                                __stcg(mine + 1 + k, tot[k]);
+                        // release: this CTA's phase writes (ordered by the
+                        // block barrier) and the values above
+                        st_release_u64(reinterpret_cast<unsigned long long *>(mine), epoch);
+                }
+                if (threadIdx.x < 32) {
+                        // wait for every CTA's tag of this epoch (bounded)
+                        int lane = threadIdx.x;
+                        unsigned pending = 0;
+                        for (unsigned q = 0, b = lane; b < nb; q++, b += 32)
+                                pending |= 1u << q;
+                        unsigned long long t0 = 0;
+                        int bad_local = 0;
+                        for (unsigned rounds = 0;; rounds++) {
+                                // relaxed loads, all in flight at once; one
+                                // acquire fence once every tag is seen
+                                for (unsigned q0 = 0; q0 * 32u < nb; q0 += 8) {
+                                        unsigned long long t[8];
+#pragma unroll
+                                        for (int j = 0; j < 8; j++) {
+                                                unsigned q = q0 + j, b = lane + 32u * q;
+                                                t[j] = (b < nb && ((pending >> q) & 1u))
+                                                        ? ld_relaxed_u64(reinterpret_cast<const unsigned long long *>(
+                                                                  lines + (size_t)b * kSlotStride))
+                                                        : epoch;
                                         }
+#pragma unroll
+                                        for (int j = 0; j < 8; j++)
+                                                if (t[j] == epoch)
+                                                        pending &= ~(1u << (q0 + j));
+                                }
+                                if (!__any_sync(0xffffffffu, pending != 0))
+                                        break;
+                                __nanosleep(16);
+                                if ((rounds & 63) == 63) {
+                                        if (lane == 0) {
+                                                if (t0 == 0)
+                                                        t0 = global_ns();
+                                                if (ld_acquire_int(status()) != 0)
+                                                        bad_local = 1;
+                                                else if (global_ns() - t0 > kWaitLimitNs) {
+                                                        fail(kStatusTimeout);
+                                                        bad_local = 1;
+                                                }
+                                        }
+                                        if (__shfl_sync(0xffffffffu, bad_local, 0))
+                                                break;
                                 }
                         }
+                        fence_acquire_gpu();
                 }
                 __syncthreads();
-                if (threadIdx.x == 0) {
-                        __threadfence();
-                        bad = ld_acquire_int(&ctl->status) != 0;
+                // warp k sums value k over all CTAs: each lane first issues all
+                // its loads (CTAs lane, lane+32, ...), then combines them in
+                // that fixed order, then a fixed shuffle tree
+                {
+                        int lane = threadIdx.x & 31, wk = threadIdx.x >> 5;
+#pragma unroll
+                        for (int k = 0; k < K; k++) {
+                                if (wk != k)
+                                        continue;
+                                double idv = red_identity(op[k]);
+                                double vals[8];
+#pragma unroll
+                                for (int q = 0; q < 8; q++) {
+                                        unsigned b = lane + 32u * q;
+                                        vals[q] = (b < nb) ? __ldcg(lines + (size_t)b * kSlotStride + 1 + k)
+                                                           : idv;
+                                }
+                                double acc = idv;
+#pragma unroll
+                                for (int q = 0; q < 8; q++)
+                                        acc = red_combine(op[k], acc, vals[q]);
+                                for (unsigned b = lane + 256u; b < nb; b += 32)
+                                        acc = red_combine(op[k], acc,
+                                                          __ldcg(lines + (size_t)b * kSlotStride + 1 + k));
+                                acc = warp_reduce(acc, op[k]);
+                                if (lane == 0)
+                                        tot[k] = acc;
+                        }
                 }
-                if (threadIdx.x < K)
-                        tot[threadIdx.x] = __ldcg(result + parity * kRedMax + threadIdx.x);
+                if (threadIdx.x == 0)
+                        bad = ld_acquire_int(status()) != 0;
                 __syncthreads();
 #pragma unroll
                 for (int k = 0; k < K; k++)
                         v[k] = tot[k];
+                int b = bad;
                 parity ^= 1;
-                return !bad;
+                return !b;
         }
 
         __device__ bool sync()
@@ -260,16 +326,83 @@ struct BlockTeam {
         }
 };
 
-// A SELL operator on the device: slice s holds rows [32s, 32s+32), element
-// (lane r, slot k) at ptr[s] + 32k + r.
+// A SELL operator on the device (layout.h: Sell).  Slice s starts at
+// element ptr[s] & ~31 and holds 32 >> c rows from row0[s], each spread over
+// L = 1 << c lanes, c = ptr[s] & 31; element k of its r-th row is at step
+// k >> c, lane (r << c) + (k & (L - 1)).
 template <class V>
 struct SellDev {
         int nrows;
         int nslices;
         const int64_t * ptr;
+        const int32_t * row0;
         const int32_t * col;
         const V * val;
 };
+
+// One warp's view of one slice.
+struct Slice {
+        int64_t base;   // first element
+        int steps;      // 32-element steps
+        int shift;      // log2(lanes per row)
+        int row;        // this lane's row (may be >= nrows: padding)
+        bool lead;      // this lane owns its row's result
+};
+
+template <class V>
+__device__ __forceinline__ Slice slice_of(const SellDev<V> & op, int s, int lane)
+{
+        Slice sl;
+        int64_t p0 = __ldg(op.ptr + s), p1 = __ldg(op.ptr + s + 1);
+        sl.shift = (int)(p0 & 31);
+        sl.base = p0 & ~int64_t(31);
+        sl.steps = (int)(((p1 & ~int64_t(31)) - sl.base) >> 5);
+        sl.row = __ldg(op.row0 + s) + (lane >> sl.shift);
+        sl.lead = (lane & ((1 << sl.shift) - 1)) == 0;
+        return sl;
+}
+
+// Visits slices so each warp of the team gets a balanced share: slices come
+// in decreasing width, and are dealt in snake order (0..W-1, W-1..0, ...).
+template <class Team, class F>
+__device__ __forceinline__ void for_each_slice(const Team & tm, int nslices, F && f)
+{
+        int w = tm.warp(), W = tm.nwarps();
+        for (int round = 0;; round++) {
+                int s = round * W + ((round & 1) ? W - 1 - w : w);
+                if (round * W >= nslices)
+                        break;
+                if (s < nslices)
+                        f(s);
+        }
+}
+
+// Sum of the L = 1 << shift lanes of each row group, into its first lane, by
+// a fixed tree.
+template <class T>
+__device__ __forceinline__ T lanes_tree(T v, int shift)
+{
+        for (int o = (1 << shift) >> 1; o > 0; o >>= 1)
+                v += __shfl_down_sync(0xffffffffu, v, o, 1 << shift);
+        return v;
+}
+
+// acc (valid in each group's first lane) += the group's L products in lane
+// order, each addition rounded: the sequential order of the row.
+__device__ __forceinline__ double lanes_in_order(double acc, double prod, int shift, int lane)
+{
+        int L = 1 << shift, first = lane & ~(L - 1);
+        for (int q = 0; q < L; q++)
+                acc = __dadd_rn(acc, __shfl_sync(0xffffffffu, prod, first + q));
+        return acc;
+}
+__device__ __forceinline__ float lanes_in_order(float acc, float prod, int shift, int lane)
+{
+        int L = 1 << shift, first = lane & ~(L - 1);
+        for (int q = 0; q < L; q++)
+                acc = __fadd_rn(acc, __shfl_sync(0xffffffffu, prod, first + q));
+        return acc;
+}
 
 // Multiply-add used by the row sums: fused (default) or the reference's
 // separate rounding of product and sum (Exact), which reproduces its bits.
@@ -289,42 +422,46 @@ __device__ __forceinline__ float madd(float a, float b, float c)
         return fmaf(a, b, c);
 }
 
-// Long rows (more than this many nonzeros) in FP32 accumulate with a
-// compensated (two-sum) sum.
+__device__ __forceinline__ double mul_exact(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mul_exact(float a, float b) { return __fmul_rn(a, b); }
+
+// Rows longer than this, in FP32, combine their lanes' partial sums in FP64
+// (a compensated sum of the row).
 constexpr int kCompensateWidth = 256;
 
-template <class T>
-struct Acc {
-        T s, c;
-        __device__ __forceinline__ void init() { s = 0; c = 0; }
-};
+// Finishes a row sum held as per-lane partials: tree (fast) or nothing (the
+// exact path accumulated in order already).
+template <bool Exact, class T>
+__device__ __forceinline__ T finish_row(T acc, int shift, int steps)
+{
+        if (Exact || shift == 0)
+                return acc;
+        if (sizeof(T) == 4 && (steps << shift) > kCompensateWidth)
+                return (T)lanes_tree((double)acc, shift);
+        return lanes_tree(acc, shift);
+}
 
-// Row sums of one SELL operator applied to x (one lane per row); calls
-// epi(row, sum) for every live row.  Rows are visited slice by slice, the
-// team's warps taking slices round-robin.
+// Row sums of one SELL operator applied to x; calls epi(row, sum) in the
+// row's lead lane for every live row.
 template <bool Exact, class Team, class V, class T, class Epi>
 __device__ __forceinline__ void sell_rows_1(const Team & tm, const SellDev<V> & op,
                                             const T * x, Epi && epi)
 {
         int lane = threadIdx.x & 31;
-        for (int s = tm.warp(); s < op.nslices; s += tm.nwarps()) {
-                int64_t base = op.ptr[s];
-                int w = (int)((op.ptr[s + 1] - base) >> 5);
-                const int32_t * cp = op.col + base + lane;
-                const V * vp = op.val + base + lane;
+        for_each_slice(tm, op.nslices, [&](int s) {
+                Slice sl = slice_of(op, s, lane);
+                const int32_t * cp = op.col + sl.base + lane;
+                const V * vp = op.val + sl.base + lane;
                 T acc = 0;
-                if (sizeof(T) == 4 && w > kCompensateWidth) {
-                        T comp = 0;
-                        for (int k = 0; k < w; k++) {
-                                T prod = (T)__ldg(vp + 32 * k) * tm.ld(x + __ldg(cp + 32 * k));
-                                T y = prod - comp;
-                                T t = acc + y;
-                                comp = (t - acc) - y;
-                                acc = t;
+                if (Exact && sl.shift) {
+                        for (int k = 0; k < sl.steps; k++) {
+                                T prod = mul_exact((T)__ldg(vp + 32 * k),
+                                                   tm.ld(x + __ldg(cp + 32 * k)));
+                                acc = lanes_in_order(acc, prod, sl.shift, lane);
                         }
                 } else {
                         int k = 0;
-                        for (; k + 4 <= w; k += 4) {
+                        for (; k + 4 <= sl.steps; k += 4) {
                                 int c0 = __ldg(cp + 32 * k), c1 = __ldg(cp + 32 * (k + 1)),
                                     c2 = __ldg(cp + 32 * (k + 2)), c3 = __ldg(cp + 32 * (k + 3));
                                 T v0 = (T)__ldg(vp + 32 * k), v1 = (T)__ldg(vp + 32 * (k + 1)),
@@ -336,14 +473,14 @@ __device__ __forceinline__ void sell_rows_1(const Team & tm, const SellDev<V> & 
                                 acc = madd<Exact>(v2, x2, acc);
                                 acc = madd<Exact>(v3, x3, acc);
                         }
-                        for (; k < w; k++)
+                        for (; k < sl.steps; k++)
                                 acc = madd<Exact>((T)__ldg(vp + 32 * k),
                                                   tm.ld(x + __ldg(cp + 32 * k)), acc);
+                        acc = finish_row<Exact>(acc, sl.shift, sl.steps);
                 }
-                int row = s * 32 + lane;
-                if (row < op.nrows)
-                        epi(row, acc);
-        }
+                if (sl.lead && sl.row < op.nrows)
+                        epi(sl.row, acc);
+        });
 }
 
 // Two right-hand sides sharing one pass over the operator.
@@ -352,27 +489,21 @@ __device__ __forceinline__ void sell_rows_2(const Team & tm, const SellDev<V> & 
                                             const T * x0, const T * x1, Epi && epi)
 {
         int lane = threadIdx.x & 31;
-        for (int s = tm.warp(); s < op.nslices; s += tm.nwarps()) {
-                int64_t base = op.ptr[s];
-                int w = (int)((op.ptr[s + 1] - base) >> 5);
-                const int32_t * cp = op.col + base + lane;
-                const V * vp = op.val + base + lane;
+        for_each_slice(tm, op.nslices, [&](int s) {
+                Slice sl = slice_of(op, s, lane);
+                const int32_t * cp = op.col + sl.base + lane;
+                const V * vp = op.val + sl.base + lane;
                 T a0 = 0, a1 = 0;
-                if (sizeof(T) == 4 && w > kCompensateWidth) {
-                        T c0 = 0, c1 = 0;
-                        for (int k = 0; k < w; k++) {
+                if (Exact && sl.shift) {
+                        for (int k = 0; k < sl.steps; k++) {
                                 int c = __ldg(cp + 32 * k);
                                 T v = (T)__ldg(vp + 32 * k);
-                                T y0 = v * tm.ld(x0 + c) - c0, t0 = a0 + y0;
-                                c0 = (t0 - a0) - y0;
-                                a0 = t0;
-                                T y1 = v * tm.ld(x1 + c) - c1, t1 = a1 + y1;
-                                c1 = (t1 - a1) - y1;
-                                a1 = t1;
+                                a0 = lanes_in_order(a0, mul_exact(v, tm.ld(x0 + c)), sl.shift, lane);
+                                a1 = lanes_in_order(a1, mul_exact(v, tm.ld(x1 + c)), sl.shift, lane);
                         }
                 } else {
                         int k = 0;
-                        for (; k + 2 <= w; k += 2) {
+                        for (; k + 2 <= sl.steps; k += 2) {
                                 int c0 = __ldg(cp + 32 * k), c1 = __ldg(cp + 32 * (k + 1));
                                 T v0 = (T)__ldg(vp + 32 * k), v1 = (T)__ldg(vp + 32 * (k + 1));
                                 T p0 = tm.ld(x0 + c0), q0 = tm.ld(x1 + c0);
@@ -382,17 +513,18 @@ __device__ __forceinline__ void sell_rows_2(const Team & tm, const SellDev<V> & 
                                 a0 = madd<Exact>(v1, p1, a0);
                                 a1 = madd<Exact>(v1, q1, a1);
                         }
-                        for (; k < w; k++) {
+                        for (; k < sl.steps; k++) {
                                 int c = __ldg(cp + 32 * k);
                                 T v = (T)__ldg(vp + 32 * k);
                                 a0 = madd<Exact>(v, tm.ld(x0 + c), a0);
                                 a1 = madd<Exact>(v, tm.ld(x1 + c), a1);
                         }
+                        a0 = finish_row<Exact>(a0, sl.shift, sl.steps);
+                        a1 = finish_row<Exact>(a1, sl.shift, sl.steps);
                 }
-                int row = s * 32 + lane;
-                if (row < op.nrows)
-                        epi(row, a0, a1);
-        }
+                if (sl.lead && sl.row < op.nrows)
+                        epi(sl.row, a0, a1);
+        });
 }
 
 }  // namespace acd

@@ -25,6 +25,7 @@ struct DevInstance {
         // SELL operators (FP64 values)
         int a_nslices = 0, at_nslices = 0;
         int64_t * a_ptr = nullptr, * at_ptr = nullptr;
+        int32_t * a_row0 = nullptr, * at_row0 = nullptr;
         int32_t * a_col = nullptr, * at_col = nullptr;
         double * a_val = nullptr, * at_val = nullptr;
         int max_width_a = 0, max_width_at = 0;
@@ -128,6 +129,9 @@ struct ScratchSolve {
 // Bytes of the control region of a ScratchSolve for max_blocks CTAs
 // (everything but the vectors).
 size_t scratch_control_bytes(int max_blocks);
+// Lays out the control region (scratch_control_bytes(max_blocks) bytes at
+// base) into s: control words, reduction slots, result, output, log count.
+void carve_control(char * base, int max_blocks, ScratchSolve & s);
 
 // approx_solve from a device array x (n doubles, original order, updated in
 // place) with every piece of solver scratch in `s`; the instance's device

@@ -268,63 +268,92 @@ std::vector<int32_t> order_by_length(const std::vector<uint32_t> & ptr)
         return order;
 }
 
-// One SELL operator: device row d is CSR row src_of_d[d]; its entries keep
-// their CSR order, columns mapped through col_map (identity if empty).
+// Lanes per row for a slice whose longest row has `len` entries.
+int lanes_for(uint32_t len)
+{
+        if (len <= 32)
+                return 1;
+        if (len <= 128)
+                return 4;
+        if (len <= 512)
+                return 16;
+        return 32;
+}
+
+int log2i(int v)
+{
+        int r = 0;
+        while ((1 << r) < v)
+                r++;
+        return r;
+}
+
+// One SELL operator: device row d is CSR row src_of_d[d] (rows already in
+// decreasing length); its entries keep their CSR order, columns mapped
+// through col_map (identity if empty).
 void build_sell(Sell & s, const Csr & c, const std::vector<int32_t> & src_of_d,
                 const std::vector<int32_t> & col_map)
 {
         int n = (int)src_of_d.size();
         s.nrows = n;
-        s.nslices = (n + kSlice - 1) / kSlice;
-        s.ptr.assign(s.nslices + 1, 0);
+        s.ptr.clear();
+        s.row0.clear();
         s.max_width = 0;
-        for (int sl = 0; sl < s.nslices; sl++) {
+        auto len_of = [&](int d) { return c.ptr[src_of_d[d] + 1] - c.ptr[src_of_d[d]]; };
+        std::vector<int> lanes;
+        int64_t off = 0;
+        for (int d = 0; d < n;) {
+                uint32_t first = len_of(d);
+                int L = lanes_for(first);
+                int h = kSlice / L;
                 uint32_t w = 0;
-                for (int d = sl * kSlice; d < std::min(n, (sl + 1) * kSlice); d++) {
-                        int r = src_of_d[d];
-                        w = std::max(w, c.ptr[r + 1] - c.ptr[r]);
-                }
+                for (int r = d; r < std::min(n, d + h); r++)
+                        w = std::max(w, len_of(r));
                 s.max_width = std::max(s.max_width, (int)w);
-                s.ptr[sl + 1] = s.ptr[sl] + (int64_t)w * kSlice;
+                int steps = (int)((w + L - 1) / L);
+                s.ptr.push_back(off | log2i(L));
+                s.row0.push_back(d);
+                lanes.push_back(L);
+                off += (int64_t)steps * kSlice;
+                d += h;
         }
-        s.col.assign(s.ptr[s.nslices], 0);
-        s.val.assign(s.ptr[s.nslices], 0.0);
+        s.nslices = (int)s.row0.size();
+        s.ptr.push_back(off);
+        s.col.assign(off, 0);
+        s.val.assign(off, 0.0);
+        auto map = [&](uint32_t cc) {
+                return col_map.empty() ? (int32_t)cc : col_map[cc];
+        };
         for (int sl = 0; sl < s.nslices; sl++) {
-                int64_t base = s.ptr[sl];
-                int w = (int)((s.ptr[sl + 1] - base) / kSlice);
+                int64_t base = s.ptr[sl] & ~int64_t(31);
+                int L = lanes[sl], h = kSlice / L;
+                int steps = (int)(((s.ptr[sl + 1] & ~int64_t(31)) - base) / kSlice);
+                int d0 = s.row0[sl];
                 int32_t slice_pad = 0;
-                for (int lane = 0; lane < kSlice; lane++) {
-                        int d = sl * kSlice + lane;
-                        if (d >= n)
-                                break;
-                        int r = src_of_d[d];
-                        if (c.ptr[r + 1] > c.ptr[r]) {
-                                uint32_t j = c.ptr[r];
-                                slice_pad = col_map.empty()
-                                        ? (int32_t)c.col[j] : col_map[c.col[j]];
+                for (int r = 0; r < h && d0 + r < n; r++) {
+                        int src = src_of_d[d0 + r];
+                        if (c.ptr[src + 1] > c.ptr[src]) {
+                                slice_pad = map(c.col[c.ptr[src]]);
                                 break;
                         }
                 }
-                for (int lane = 0; lane < kSlice; lane++) {
-                        int d = sl * kSlice + lane;
+                for (int r = 0; r < h; r++) {
+                        int d = d0 + r;
                         int32_t pad = slice_pad;
-                        int k = 0;
+                        uint32_t k = 0;
                         if (d < n) {
-                                int r = src_of_d[d];
-                                for (uint32_t j = c.ptr[r]; j < c.ptr[r + 1];
-                                     j++, k++) {
-                                        int32_t cc = col_map.empty()
-                                                ? (int32_t)c.col[j]
-                                                : col_map[c.col[j]];
-                                        s.col[base + (int64_t)k * kSlice + lane] = cc;
-                                        s.val[base + (int64_t)k * kSlice + lane] = c.val[j];
-                                        pad = cc;
+                                int src = src_of_d[d];
+                                for (uint32_t j = c.ptr[src]; j < c.ptr[src + 1]; j++, k++) {
+                                        int64_t at = base + (int64_t)(k / L) * kSlice + r * L + k % L;
+                                        s.col[at] = map(c.col[j]);
+                                        s.val[at] = c.val[j];
+                                        pad = s.col[at];
                                 }
                         }
-                        // Padding: value 0, a column of this row (or slice),
-                        // so the gather stays in cache and in bounds.
-                        for (; k < w; k++)
-                                s.col[base + (int64_t)k * kSlice + lane] = pad;
+                        // padding: value 0, a column of this row (or slice),
+                        // so the gather stays in cache and in bounds
+                        for (; k < (uint32_t)steps * L; k++)
+                                s.col[base + (int64_t)(k / L) * kSlice + r * L + k % L] = pad;
                 }
         }
 }

@@ -56,12 +56,19 @@ void build_matrix(HostMatrix & m, size_t ncols, size_t nrows, size_t nnz,
 void ensure_blocks(HostMatrix & m);
 void ensure_zorder(HostMatrix & m);
 
-// Warp-sliced ELL of one operator (A or A') in device order.
+// Warp-sliced ELL of one operator (A or A') in device order, with a
+// per-slice height.  A slice is 32 lanes wide; it holds h = 32 / L
+// consecutive rows, each row spread over L lanes (L = 1, 4, 16 or 32, chosen
+// from the slice's longest row so no slice needs more than ~32 steps).
+// Element k of the slice's r-th row sits at step k / L, lane r * L + k % L,
+// i.e. at offset ptr + 32 * (k / L) + r * L + k % L.  ptr is a multiple of
+// 32; its low 5 bits hold log2(L).
 struct Sell {
         int nrows = 0;                 // rows of the operator
-        int nslices = 0;               // ceil(nrows / 32)
-        std::vector<int64_t> ptr;      // nslices + 1, element offsets
-        std::vector<int32_t> col;      // ptr[nslices]
+        int nslices = 0;
+        std::vector<int64_t> ptr;      // nslices + 1: element offset | log2(L)
+        std::vector<int32_t> row0;     // nslices: first row of each slice
+        std::vector<int32_t> col;      // ptr[nslices] >> 5 << 5
         std::vector<double> val;
         int max_width = 0;
 };

@@ -17,6 +17,7 @@ namespace acd {
 namespace {
 
 constexpr int kThreads = 256;
+constexpr int kMaxTeamCtas = 1024;  // GridTeam's per-lane wait mask covers 32 x 32 CTAs
 constexpr int kLogCap = 1 << 14;
 
 // ---- small kernels ------------------------------------------------------
@@ -50,16 +51,16 @@ __global__ void step_size_kernel(SellDev<double> at, const double * w,
         int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
         int nwarps = (gridDim.x * blockDim.x) >> 5;
         for (int s = warp; s < at.nslices; s += nwarps) {
-                int64_t base = at.ptr[s];
-                int wd = (int)((at.ptr[s + 1] - base) >> 5);
+                Slice sl = slice_of(at, s, lane);
                 double acc = 0;
-                for (int k = 0; k < wd; k++) {
-                        int i = at.col[base + 32 * k + lane];
-                        double a = at.val[base + 32 * k + lane];
-                        acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(__dmul_rn(w[i], beta[i]), a), a));
+                for (int k = 0; k < sl.steps; k++) {
+                        int i = at.col[sl.base + 32 * k + lane];
+                        double a = at.val[sl.base + 32 * k + lane];
+                        double t = __dmul_rn(__dmul_rn(__dmul_rn(w[i], beta[i]), a), a);
+                        acc = lanes_in_order(acc, t, sl.shift, lane);
                 }
-                int j = s * 32 + lane;
-                if (j < at.nrows) {
+                int j = sl.row;
+                if (sl.lead && j < at.nrows) {
                         v[j] = acc;
                         inv_v[j] = (acc == 0 && c[j] == 0) ? 1.0 : 1.0 / acc;
                 }
@@ -80,9 +81,9 @@ struct AlmKernelArgs {
 };
 
 template <bool Exact>
-__global__ void __launch_bounds__(kThreads, 1) alm_kernel(AlmKernelArgs k)
+__global__ void __launch_bounds__(kThreads, 2) alm_kernel(AlmKernelArgs k)
 {
-        GridTeam tm{k.ctl, k.slots, k.result, 0};
+        GridTeam tm{k.ctl, k.slots, k.result, 0, 0u};
         Alm<GridTeam, Exact> alm(tm, k.P, k.W, k.log);
         AlmOut out;
         memset(&out, 0, sizeof(out));
@@ -113,9 +114,9 @@ struct ApproxKernelArgs {
 };
 
 template <bool Exact>
-__global__ void __launch_bounds__(kThreads, 1) approx_kernel(ApproxKernelArgs k)
+__global__ void __launch_bounds__(kThreads, 2) approx_kernel(ApproxKernelArgs k)
 {
-        GridTeam tm{k.ctl, k.slots, k.result, 0};
+        GridTeam tm{k.ctl, k.slots, k.result, 0, 0u};
         Approx<double, GridTeam, Exact> ap(tm, k.P, k.W, k.log);
         ApproxOut out;
         memset(&out, 0, sizeof(out));
@@ -252,9 +253,9 @@ struct Spg {
         }
 };
 
-__global__ void __launch_bounds__(kThreads, 1) mpg_kernel(ApproxKernelArgs k)
+__global__ void __launch_bounds__(kThreads, 2) mpg_kernel(ApproxKernelArgs k)
 {
-        GridTeam tm{k.ctl, k.slots, k.result, 0};
+        GridTeam tm{k.ctl, k.slots, k.result, 0, 0u};
         Approx<double, GridTeam, false> ap(tm, k.P, k.W, k.log);
         Spg<GridTeam, false> spg(ap);
         ApproxOut out;
@@ -433,12 +434,12 @@ InnerWork<double> work_of(DevInstance & d)
 
 SellDev<double> sell_a(const DevInstance & d)
 {
-        return {d.m, d.a_nslices, d.a_ptr, d.a_col, d.a_val};
+        return {d.m, d.a_nslices, d.a_ptr, d.a_row0, d.a_col, d.a_val};
 }
 
 SellDev<double> sell_at(const DevInstance & d)
 {
-        return {d.n, d.at_nslices, d.at_ptr, d.at_col, d.at_val};
+        return {d.n, d.at_nslices, d.at_ptr, d.at_row0, d.at_col, d.at_val};
 }
 
 int reset_ctl(DevInstance & d)
@@ -450,9 +451,10 @@ int reset_ctl(DevInstance & d)
 
 int read_status(DevInstance & d, int & status)
 {
-        TeamCtl c;
-        ACD_CUDA_TRY(cudaMemcpy(&c, d.ctl, sizeof(c), cudaMemcpyDeviceToHost), ACDALM_ECUDA);
-        status = c.status;
+        int s = 0;
+        ACD_CUDA_TRY(cudaMemcpy(&s, &static_cast<TeamCtl *>(d.ctl)->status_w.v, sizeof(int),
+                                cudaMemcpyDeviceToHost), ACDALM_ECUDA);
+        status = s;
         return 0;
 }
 
@@ -471,7 +473,7 @@ int launch_coop(const void * fn, int max_blocks, void * args, cudaStream_t s)
 {
         // every CTA must be resident at once: never more than the occupancy
         // of this kernel allows, nor more than the reduction slots hold
-        int blocks = std::min(max_blocks, launch_blocks(fn));
+        int blocks = std::min(std::min(max_blocks, launch_blocks(fn)), kMaxTeamCtas);
         void * params[1] = {args};
         ACD_CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kThreads),
                                                  params, 0, s), ACDALM_ECUDA);
@@ -498,14 +500,15 @@ int DevInstance::create(const DeviceLayout & lay)
                                        launch_blocks((const void *)mpg_kernel)));
         grid_blocks = blocks;
         size_t ea = lay.a.ptr.back(), eat = lay.at.ptr.back();
+        size_t sa = std::max<size_t>(lay.a.row0.size(), 1), sat = std::max<size_t>(lay.at.row0.size(), 1);
         size_t mm = std::max(m, 1), nn = std::max(n, 1);
         size_t total = 0;
-        total += rounded((lay.a.ptr.size()) * 8) + rounded(ea * 4) + rounded(ea * 8);
-        total += rounded((lay.at.ptr.size()) * 8) + rounded(eat * 4) + rounded(eat * 8);
+        total += rounded((lay.a.ptr.size()) * 8) + rounded(sa * 4) + rounded(ea * 4) + rounded(ea * 8);
+        total += rounded((lay.at.ptr.size()) * 8) + rounded(sat * 4) + rounded(eat * 4) + rounded(eat * 8);
         total += rounded(mm * 4) + rounded(nn * 4) + rounded(mm * 8);
         total += 6 * rounded(mm * 8) + 7 * rounded(nn * 8);
         total += 9 * rounded(nn * 8) + 6 * rounded(mm * 8);
-        total += rounded(sizeof(TeamCtl)) + rounded(2 * (size_t)blocks * kRedMax * 8)
+        total += rounded(sizeof(TeamCtl)) + rounded(2 * (size_t)blocks * kSlotStride * 8)
                 + rounded(2 * kRedMax * 8);
         log_cap = kLogCap;
         total += rounded((size_t)log_cap * sizeof(LogRec)) + rounded(sizeof(int));
@@ -521,9 +524,11 @@ int DevInstance::create(const DeviceLayout & lay)
         bytes = total;
         char * p = static_cast<char *>(mem);
         a_ptr = carve<int64_t>(p, lay.a.ptr.size());
+        a_row0 = carve<int32_t>(p, sa);
         a_col = carve<int32_t>(p, ea);
         a_val = carve<double>(p, ea);
         at_ptr = carve<int64_t>(p, lay.at.ptr.size());
+        at_row0 = carve<int32_t>(p, sat);
         at_col = carve<int32_t>(p, eat);
         at_val = carve<double>(p, eat);
         row_orig = carve<int32_t>(p, mm);
@@ -547,7 +552,7 @@ int DevInstance::create(const DeviceLayout & lay)
         for (auto & q : wm)
                 q = carve<double>(p, mm);
         ctl = carve<TeamCtl>(p, 1);
-        slots = carve<double>(p, 2 * (size_t)blocks * kRedMax);
+        slots = carve<double>(p, 2 * (size_t)blocks * kSlotStride);
         result = carve<double>(p, 2 * kRedMax);
         log = carve<LogRec>(p, log_cap);
         log_count = carve<int>(p, 1);
@@ -559,9 +564,11 @@ int DevInstance::create(const DeviceLayout & lay)
                           : cudaSuccess;
         };
         ACD_CUDA_TRY(up(a_ptr, lay.a.ptr.data(), lay.a.ptr.size() * 8), ACDALM_ECUDA);
+        ACD_CUDA_TRY(up(a_row0, lay.a.row0.data(), lay.a.row0.size() * 4), ACDALM_ECUDA);
         ACD_CUDA_TRY(up(a_col, lay.a.col.data(), ea * 4), ACDALM_ECUDA);
         ACD_CUDA_TRY(up(a_val, lay.a.val.data(), ea * 8), ACDALM_ECUDA);
         ACD_CUDA_TRY(up(at_ptr, lay.at.ptr.data(), lay.at.ptr.size() * 8), ACDALM_ECUDA);
+        ACD_CUDA_TRY(up(at_row0, lay.at.row0.data(), lay.at.row0.size() * 4), ACDALM_ECUDA);
         ACD_CUDA_TRY(up(at_col, lay.at.col.data(), eat * 4), ACDALM_ECUDA);
         ACD_CUDA_TRY(up(at_val, lay.at.val.data(), eat * 8), ACDALM_ECUDA);
         ACD_CUDA_TRY(up(row_orig, lay.row_orig_of_d.data(), (size_t)m * 4), ACDALM_ECUDA);
@@ -785,8 +792,19 @@ static int run_inner(DevInstance & d, const HostVectors & hv, double * x,
 
 size_t scratch_control_bytes(int max_blocks)
 {
-        return rounded(sizeof(TeamCtl)) + rounded(2 * (size_t)max_blocks * kRedMax * 8)
+        return rounded(sizeof(TeamCtl)) + rounded(2 * (size_t)max_blocks * kSlotStride * 8)
                 + rounded(2 * kRedMax * 8) + rounded(sizeof(ApproxOut)) + rounded(sizeof(int));
+}
+
+void carve_control(char * base, int max_blocks, ScratchSolve & s)
+{
+        char * p = base;
+        s.max_blocks = max_blocks;
+        s.ctl = carve<TeamCtl>(p, 1);
+        s.slots = carve<double>(p, 2 * (size_t)max_blocks * kSlotStride);
+        s.result = carve<double>(p, 2 * kRedMax);
+        s.out = carve<ApproxOut>(p, 1);
+        s.log_count = carve<int>(p, 1);
 }
 
 int run_approx_scratch(DevInstance & d, const HostVectors & hv, double * x_dev,
@@ -864,16 +882,17 @@ int run_approx_scratch(DevInstance & d, const HostVectors & hv, double * x_dev,
                 count_launch();
                 ACD_CUDA_TRY(cudaGetLastError(), ACDALM_ECUDA);
         }
-        TeamCtl c;
+        int status = 0;
         ApproxOut out;
-        ACD_CUDA_TRY(cudaMemcpyAsync(&c, s.ctl, sizeof(c), cudaMemcpyDeviceToHost, stream),
+        ACD_CUDA_TRY(cudaMemcpyAsync(&status, &static_cast<TeamCtl *>(s.ctl)->status_w.v,
+                                     sizeof(int), cudaMemcpyDeviceToHost, stream),
                      ACDALM_ECUDA);
         ACD_CUDA_TRY(cudaMemcpyAsync(&out, s.out, sizeof(out), cudaMemcpyDeviceToHost, stream),
                      ACDALM_ECUDA);
         ACD_CUDA_TRY(cudaStreamSynchronize(stream), ACDALM_ECUDA);
-        if (c.status != 0) {
-                set_error(c.status, "device solve failed with status %d", c.status);
-                return c.status;
+        if (status != 0) {
+                set_error(status, "device solve failed with status %d", status);
+                return status;
         }
         if (diag5)
                 for (int i = 0; i < 5; i++)

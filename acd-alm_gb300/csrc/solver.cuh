@@ -761,32 +761,39 @@ struct Alm {
         // where v = 0 and c = 0).  Partials: lambda'b, and the relative KKT
         // terms of (x, lambda) when kkt is set.
         __device__ bool penalise(const double * lam, const double * x, bool kkt,
-                                 double (&out)[6])
+                                 double (&out)[6], bool write = true)
         {
                 double part[6] = {0, 0, 0, 0, 0, 0};
                 const int op[6] = {RED_SUM, RED_SUM, RED_SUM, RED_SUM, RED_SUM, RED_SUM};
                 int lane = threadIdx.x & 31;
                 const SellDev<double> & op_t = P.At;
-                for (int s = tm.warp(); s < op_t.nslices; s += tm.nwarps()) {
-                        int64_t base = op_t.ptr[s];
-                        int wdt = (int)((op_t.ptr[s + 1] - base) >> 5);
-                        const int32_t * cp = op_t.col + base + lane;
-                        const double * vp = op_t.val + base + lane;
+                for_each_slice(tm, op_t.nslices, [&](int s) {
+                        Slice sl = slice_of(op_t, s, lane);
+                        const int32_t * cp = op_t.col + sl.base + lane;
+                        const double * vp = op_t.val + sl.base + lane;
                         double acc = 0, vv = 0;
-                        for (int k = 0; k < wdt; k++) {
+                        for (int k = 0; k < sl.steps; k++) {
                                 int i = __ldg(cp + 32 * k);
                                 double a = __ldg(vp + 32 * k);
-                                acc = madd<Exact>(a, tm.ld(lam + i), acc);
+                                // v in the reference's order and rounding
                                 double t = __dmul_rn(__dmul_rn(__dmul_rn(tm.ld(P.w + i),
                                                                          P.beta[i]), a), a);
-                                vv = __dadd_rn(vv, t);
+                                vv = lanes_in_order(vv, t, sl.shift, lane);
+                                if (Exact)
+                                        acc = lanes_in_order(acc, __dmul_rn(a, tm.ld(lam + i)),
+                                                             sl.shift, lane);
+                                else
+                                        acc = fma(a, tm.ld(lam + i), acc);
                         }
-                        int j = s * 32 + lane;
-                        if (j < P.n) {
+                        acc = finish_row<Exact>(acc, sl.shift, sl.steps);
+                        int j = sl.row;
+                        if (sl.lead && j < P.n) {
                                 double cj = P.c0[j] - acc;
-                                P.c[j] = cj;
-                                P.v[j] = vv;
-                                P.inv_v[j] = (vv == 0 && cj == 0) ? 1.0 : 1.0 / vv;
+                                if (write) {
+                                        P.c[j] = cj;
+                                        P.v[j] = vv;
+                                        P.inv_v[j] = (vv == 0 && cj == 0) ? 1.0 : 1.0 / vv;
+                                }
                                 if (kkt) {
                                         double xj = tm.ld(x + j);
                                         double xp = xj - cj;
@@ -800,7 +807,7 @@ struct Alm {
                                         part[3] += isfinite(t) ? t : 0.0;
                                 }
                         }
-                }
+                });
                 for (int i = tm.tid(); i < P.m; i += tm.nthreads()) {
                         double li = tm.ld(lam + i);
                         part[0] += li * P.b[i];
@@ -1012,8 +1019,9 @@ struct Alm {
                                 break;
                         }
                 }
-                // final relative KKT of (x, lambda)
-                if (!penalise(lam, x, true, kk))
+                // final relative KKT of (x, lambda); c, v, 1/v keep the
+                // last outer iteration's values (approx_linear, alm.c:109-116)
+                if (!penalise(lam, x, true, kk, false))
                         return -1;
                 {
                         double primal = sqrt(kk[4]) / (1 + P.bnorm);

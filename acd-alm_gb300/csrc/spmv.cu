@@ -207,12 +207,15 @@ int ensure_layout(sparse_matrix_t * a, int variant, int transpose, bool f32)
                         acd::PlainSell ps;
                         acd::build_plain_sell(a->h, transpose, ps);
                         size_t e = ps.s.ptr.back();
-                        size_t total = rnd(ps.s.ptr.size() * 8) + rnd(e * 4) + rnd(e * 8)
-                                + rnd(e * 4) + rnd(std::max<size_t>(ps.row_of_d.size(), 1) * 4);
+                        size_t ns = std::max<size_t>(ps.s.row0.size(), 1);
+                        size_t total = rnd(ps.s.ptr.size() * 8) + rnd(ns * 4) + rnd(e * 4)
+                                + rnd(e * 8) + rnd(e * 4)
+                                + rnd(std::max<size_t>(ps.row_of_d.size(), 1) * 4);
                         ACD_CUDA_TRY(cudaMalloc(&L.mem, total), ACDALM_ENOMEM);
                         L.bytes = total;
                         char * p = static_cast<char *>(L.mem);
                         int64_t * dptr = carve<int64_t>(p, ps.s.ptr.size());
+                        int32_t * drow0 = carve<int32_t>(p, ns);
                         int32_t * dcol = carve<int32_t>(p, e);
                         double * dval = carve<double>(p, e);
                         L.valf = carve<float>(p, e);
@@ -220,6 +223,9 @@ int ensure_layout(sparse_matrix_t * a, int variant, int transpose, bool f32)
                         std::vector<float> vf(ps.s.val.begin(), ps.s.val.end());
                         ACD_CUDA_TRY(cudaMemcpy(dptr, ps.s.ptr.data(), ps.s.ptr.size() * 8,
                                                 cudaMemcpyHostToDevice), ACDALM_ECUDA);
+                        if (!ps.s.row0.empty())
+                                ACD_CUDA_TRY(cudaMemcpy(drow0, ps.s.row0.data(), ps.s.row0.size() * 4,
+                                                        cudaMemcpyHostToDevice), ACDALM_ECUDA);
                         if (e) {
                                 ACD_CUDA_TRY(cudaMemcpy(dcol, ps.s.col.data(), e * 4,
                                                         cudaMemcpyHostToDevice), ACDALM_ECUDA);
@@ -232,8 +238,8 @@ int ensure_layout(sparse_matrix_t * a, int variant, int transpose, bool f32)
                                 ACD_CUDA_TRY(cudaMemcpy(L.row_of_d, ps.row_of_d.data(),
                                                         ps.row_of_d.size() * 4,
                                                         cudaMemcpyHostToDevice), ACDALM_ECUDA);
-                        L.sell = {ps.s.nrows, ps.s.nslices, dptr, dcol, dval};
-                        L.sellf = {ps.s.nrows, ps.s.nslices, dptr, dcol, L.valf};
+                        L.sell = {ps.s.nrows, ps.s.nslices, dptr, drow0, dcol, dval};
+                        L.sellf = {ps.s.nrows, ps.s.nslices, dptr, drow0, dcol, L.valf};
                 } else if (variant == ACDALM_SPMV_BLOCK) {
                         acd::ensure_blocks(a->h);
                         const acd::BlockArena & B = transpose ? a->h.block_t : a->h.block;

@@ -112,20 +112,7 @@ extern "C" int approx_solve_static(double * x, size_t n, approx_t * approx,
                 return q;
         };
         acd::ScratchSolve s;
-        s.max_blocks = kStaticBlocks;
-        size_t ctl_bytes = acd::scratch_control_bytes(kStaticBlocks);
-        char * ctl = carve(ctl_bytes);
-        // the control region, split as scratch_control_bytes() sizes it
-        char * q = ctl;
-        s.ctl = q;
-        q += 256;
-        s.slots = reinterpret_cast<double *>(q);
-        q += rounded(2 * (size_t)kStaticBlocks * 8 * 8);
-        s.result = reinterpret_cast<double *>(q);
-        q += rounded(2 * 8 * 8);
-        s.out = q;
-        q += 256;
-        s.log_count = reinterpret_cast<int *>(q);
+        acd::carve_control(carve(acd::scratch_control_bytes(kStaticBlocks)), kStaticBlocks, s);
         s.v = reinterpret_cast<double *>(carve(n * 8));
         s.inv_v = reinterpret_cast<double *>(carve(n * 8));
         s.xd = reinterpret_cast<double *>(carve(n * 8));

@@ -1503,6 +1503,9 @@ int or_alm_solve(or_alm_t * alm, size_t niter, double * x, double * lambda,
                         ret = 0;
                         break;
                 }
+                /* the inner budget is a harness stop, not the reference's */
+                if (inner_budget != (size_t)-1 && used >= inner_budget)
+                        break;
         }
         if (diag != NULL) {
                 diag[0] = sdot(x, alm->linear, alm->nvars);

@@ -243,7 +243,7 @@ int alm_solve(alm_t * m, size_t niter, double * x, size_t nvars, double * lambda
         hv.lam_lo = m->lambda_lower.data();
         hv.lam_hi = m->lambda_upper.data();
         r = acd::run_alm(a->dev, hv, niter, x, lambda, log, OUT_diagnosis, m->settings,
-                         a->weight.data(), a->linear.data(), m->stats);
+                         a->weight.data(), a->linear.data(), m->stats, &a->lay);
         if (r >= 0) {
                 // the shadow holds what the last outer iteration published
                 a->s_rhs = a->rhs;
@@ -352,6 +352,88 @@ struct approx * acdalm_alm_approx(struct alm * m)
 struct sparse_matrix * acdalm_approx_permuted_matrix(struct approx * a)
 {
         return a->permuted;
+}
+
+// ---- batches ----
+
+acdalm_batch_t * acdalm_batch_make(struct alm * const * instances, size_t count)
+{
+        if (count && !instances) {
+                acd::set_error(ACDALM_EINVAL, "acdalm_batch_make: NULL instances");
+                return nullptr;
+        }
+        for (size_t i = 0; i < count; i++)
+                if (!instances[i]) {
+                        acd::set_error(ACDALM_EINVAL, "acdalm_batch_make: instance %zu is NULL", i);
+                        return nullptr;
+                }
+        acdalm_batch_t * b = new (std::nothrow) acdalm_batch;
+        if (!b)
+                return nullptr;
+        b->alms.assign(instances, instances + count);
+        return b;
+}
+
+int acdalm_batch_free(acdalm_batch_t * b)
+{
+        delete b;
+        return 0;
+}
+
+int acdalm_batch_solve(acdalm_batch_t * b, size_t niter, double * const * x,
+                       double * const * lambda, int * ret, double * diag)
+{
+        if (!b || (b->alms.size() && (!x || !lambda))) {
+                acd::set_error(ACDALM_EINVAL, "acdalm_batch_solve: NULL arguments");
+                return ACDALM_EINVAL;
+        }
+        size_t n = b->alms.size();
+        std::vector<acd::BatchEntry> entries(n);
+        std::vector<std::unique_lock<std::mutex>> locks;
+        for (size_t i = 0; i < n; i++) {
+                alm_t * m = b->alms[i];
+                approx_t * a = m->approx;
+                locks.emplace_back(a->lock);
+                int r = ensure_device(a);
+                if (r)
+                        return r;
+                acd::BatchEntry & e = entries[i];
+                e.dev = &a->dev;
+                e.lay = &a->lay;
+                e.hv.b = a->rhs.data();
+                e.hv.w = a->weight.data();
+                e.hv.c0 = m->linear.data();
+                e.hv.l = a->lower.data();
+                e.hv.u = a->upper.data();
+                e.hv.lam_lo = m->lambda_lower.data();
+                e.hv.lam_hi = m->lambda_upper.data();
+                e.settings = m->settings;
+                e.x = x[i];
+                e.lam = lambda[i];
+                e.diag3 = diag ? diag + 3 * i : nullptr;
+                e.w_out = a->weight.data();
+                e.c_out = a->linear.data();
+                e.stats = &m->stats;
+        }
+        int r = acd::run_alm_batch(entries, niter, &b->seconds);
+        for (size_t i = 0; i < n; i++) {
+                if (ret)
+                        ret[i] = entries[i].ret;
+                approx_t * a = b->alms[i]->approx;
+                if (entries[i].ret >= 0) {
+                        a->s_rhs = a->rhs;
+                        a->s_weight = a->weight;
+                        a->s_linear = a->linear;
+                        a->s_lower = a->lower;
+                        a->s_upper = a->upper;
+                }
+        }
+        return r;
+}
+
+double acdalm_batch_seconds(acdalm_batch_t * b)
+{
+        return b ? b->seconds : 0;
 }
 
 // Step sizes as the solver computes them, in original order: beta (m), v,

@@ -289,8 +289,11 @@ struct GridTeam {
         }
 };
 
+// One CTA (one LP of a batch): barriers are __syncthreads, reductions stay
+// in shared memory, loads may use L1 (only this SM writes the LP's data).
 struct BlockTeam {
-        int * status;     // per-instance status word in global memory
+        int * status;     // the LP's status word in global memory
+
         static constexpr bool kShared = true;
 
         __device__ int nthreads() const { return blockDim.x; }
@@ -302,21 +305,17 @@ struct BlockTeam {
         __device__ bool failed() const { return *(volatile int *)status != 0; }
         __device__ void fail(int code) { atomicCAS(status, 0, code); }
 
+        // Failures of a one-CTA team are raised by its own threads, which
+        // all return at once, so the reduction needs no status check.
         template <int K>
         __device__ bool reduce(double (&v)[K], const int (&op)[K])
         {
                 __shared__ double tot[kRedMax];
-                __shared__ int bad;
                 block_reduce<K>(v, op, tot);
 #pragma unroll
                 for (int k = 0; k < K; k++)
                         v[k] = tot[k];
-                if (threadIdx.x == 0)
-                        bad = *(volatile int *)status != 0;
-                __syncthreads();
-                int b = bad;
-                __syncthreads();
-                return !b;
+                return true;
         }
 
         __device__ bool sync()

@@ -57,11 +57,20 @@ struct DevInstance {
         int grid_blocks = 0;           // cooperative grid size
         int block_threads = 256;
 
-        // host staging (pinned)
-        double * h_stage = nullptr;
-        size_t h_stage_len = 0;
+        // FP32 copies for the mixed precision mode (allocated on first use)
+        void * mem32 = nullptr;
+        size_t bytes32 = 0;
+        float * a_valf = nullptr, * at_valf = nullptr;
+        float * bf = nullptr, * wf = nullptr;                       // m
+        float * cf = nullptr, * lf = nullptr, * uf = nullptr,       // n
+              * vf = nullptr, * ivf = nullptr, * d = nullptr;
+        float * wnf[9] = {};
+        float * wmf[6] = {};
 
         int create(const DeviceLayout & lay);
+        int ensure_f32(const DeviceLayout & lay);
+        // Device bytes create() (+ ensure_f32 when mixed) would allocate.
+        static size_t footprint(const DeviceLayout & lay, bool mixed);
         void destroy();
 };
 
@@ -96,7 +105,47 @@ struct SolveStats {
 // reference's 0/1 or a negative ACDALM_E* code.
 int run_alm(DevInstance & d, const HostVectors & hv, size_t niter, double * x,
             double * lam, FILE * log, double * diag3, const AlmSettings & s,
-            double * w_out, double * c_out, SolveStats & st);
+            double * w_out, double * c_out, SolveStats & st,
+            const DeviceLayout * lay = nullptr);
+
+// One LP of a batch (run_alm_batch): its device instance, host vectors
+// and settings, and where its results go.
+struct BatchEntry {
+        DevInstance * dev = nullptr;
+        const DeviceLayout * lay = nullptr;
+        HostVectors hv;
+        AlmSettings settings;
+        double * x = nullptr;
+        double * lam = nullptr;
+        double * diag3 = nullptr;
+        double * w_out = nullptr;
+        double * c_out = nullptr;
+        SolveStats * stats = nullptr;
+        int ret = 0;
+};
+
+// Solves every entry with one persistent launch, one LP per CTA, largest
+// first.  Returns 0 or the first negative code; each entry's ret holds its
+// own outcome.  *seconds receives the device time of the launch.
+int run_alm_batch(std::vector<BatchEntry> & entries, size_t niter, double * seconds);
+
+// One asynchronous ALM solve on one CTA (the server's unit of work): the
+// launch records `done` on the instance's stream.
+struct AlmLaunch {
+        struct Impl;
+        Impl * impl;
+        cudaEvent_t done = nullptr;
+        AlmLaunch();
+        ~AlmLaunch();
+        AlmLaunch(const AlmLaunch &) = delete;
+        AlmLaunch & operator=(const AlmLaunch &) = delete;
+};
+int alm_launch_async(DevInstance & d, const HostVectors & hv, size_t niter, double * x,
+                     double * lam, const AlmSettings & s, const DeviceLayout * lay,
+                     AlmLaunch & h);
+// After `done`: status, results (x, lambda in original order) and stats.
+int alm_collect(DevInstance & d, AlmLaunch & h, double * x, double * lam, double * diag3,
+                SolveStats & st);
 
 // approx_solve on the device over the instance's uploaded vectors (b, w,
 // c0 as the linear term, l, u; step sizes recomputed).  Returns the reason

@@ -33,3 +33,8 @@ struct alm {
         acd::AlmSettings settings;
         acd::SolveStats stats;
 };
+
+struct acdalm_batch {
+        std::vector<alm_t *> alms;
+        double seconds = 0;
+};

@@ -69,6 +69,7 @@ __global__ void step_size_kernel(SellDev<double> at, const double * w,
 
 struct AlmKernelArgs {
         AlmProblem P;
+        AlmMixed M;
         InnerWork<double> W;
         LogBuf log;
         AlmArgs a;
@@ -84,7 +85,7 @@ template <bool Exact>
 __global__ void __launch_bounds__(kThreads, 2) alm_kernel(AlmKernelArgs k)
 {
         GridTeam tm{k.ctl, k.slots, k.result, 0, 0u};
-        Alm<GridTeam, Exact> alm(tm, k.P, k.W, k.log);
+        Alm<GridTeam, Exact> alm(tm, k.P, k.W, k.log, k.M);
         AlmOut out;
         memset(&out, 0, sizeof(out));
         int r = alm.solve(k.a, k.x, k.lam, out);
@@ -151,8 +152,8 @@ struct Spg {
                 double * g2 = W.g2;
                 for (int j = tm.tid(); j < P.n; j += tm.nthreads()) {
                         double xj = tm.ld(x_io + j);
-                        double lo = maxpd(P.l[j], xj);
-                        double v = minpd(lo, P.u[j]);
+                        double lo = maxpd(tm.ld(P.l + j), xj);
+                        double v = minpd(lo, tm.ld(P.u + j));
                         x.x[j] = v;
                         z[j] = v;
                 }
@@ -178,14 +179,14 @@ struct Spg {
                         // gradient at x, pg, y = x - z, u = g - g2, dots
                         double part[4] = {0, 0, 0, 0};
                         const int op[4] = {RED_SUM, RED_SUM, RED_SUM, RED_SUM};
-                        if (i > 0 || true) {
+                        {
                                 sell_rows_1<Exact>(tm, P.At, x.viol, [&](int j, double s) {
-                                        double gj = s + P.c[j];
+                                        double gj = s + tm.ld(P.c + j);
                                         g[j] = gj;
                                         double xj = tm.ld(x.x + j);
                                         double xp = xj - gj;
-                                        xp = maxpd(P.l[j], xp);
-                                        xp = minpd(P.u[j], xp);
+                                        xp = maxpd(tm.ld(P.l + j), xp);
+                                        xp = minpd(tm.ld(P.u + j), xp);
                                         double d = xj - xp;
                                         part[0] += d * d;
                                         double yj = xj - tm.ld(z + j);
@@ -204,8 +205,8 @@ struct Spg {
                                 // z = P(x - step g); swap(z, x); swap(g2, g)
                                 for (int j = tm.tid(); j < P.n; j += tm.nthreads()) {
                                         double v = tm.ld(x.x + j) - stepl * tm.ld(g + j);
-                                        v = maxpd(P.l[j], v);
-                                        v = minpd(P.u[j], v);
+                                        v = maxpd(tm.ld(P.l + j), v);
+                                        v = minpd(tm.ld(P.u + j), v);
                                         z[j] = v;
                                 }
                                 if (!tm.sync())
@@ -514,7 +515,9 @@ int DevInstance::create(const DeviceLayout & lay)
         total += rounded((size_t)log_cap * sizeof(LogRec)) + rounded(sizeof(int));
         total += rounded(std::max(sizeof(AlmOut), sizeof(ApproxOut)));
         ACD_CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), ACDALM_ECUDA);
-        cudaError_t e = cudaMalloc(&mem, total);
+        // stream-ordered allocation: no device-wide synchronisation, so a
+        // server can admit and retire instances while others run
+        cudaError_t e = cudaMallocAsync(&mem, total, stream);
         if (e != cudaSuccess) {
                 set_error(ACDALM_ENOMEM, "cudaMalloc(%zu bytes): %s", total,
                           cudaGetErrorString(e));
@@ -578,10 +581,76 @@ int DevInstance::create(const DeviceLayout & lay)
         return 0;
 }
 
+size_t DevInstance::footprint(const DeviceLayout & lay, bool mixed)
+{
+        size_t ea = lay.a.ptr.back(), eat = lay.at.ptr.back();
+        size_t sa = std::max<size_t>(lay.a.row0.size(), 1), sat = std::max<size_t>(lay.at.row0.size(), 1);
+        size_t mm = std::max(lay.m, 1), nn = std::max(lay.n, 1);
+        size_t total = rounded((lay.a.ptr.size()) * 8) + rounded(sa * 4) + rounded(ea * 4) + rounded(ea * 8);
+        total += rounded((lay.at.ptr.size()) * 8) + rounded(sat * 4) + rounded(eat * 4) + rounded(eat * 8);
+        total += rounded(mm * 4) + rounded(nn * 4) + rounded(mm * 8);
+        total += 6 * rounded(mm * 8) + 7 * rounded(nn * 8);
+        total += 9 * rounded(nn * 8) + 6 * rounded(mm * 8);
+        total += (size_t)2 << 20;  // control, slots, log ring, outputs (bounded)
+        if (mixed)
+                total += rounded(ea * 4) + rounded(eat * 4) + 2 * rounded(mm * 4) + 15 * rounded(nn * 4)
+                        + 6 * rounded(mm * 4);
+        return total;
+}
+
+int DevInstance::ensure_f32(const DeviceLayout & lay)
+{
+        if (mem32)
+                return 0;
+        size_t ea = lay.a.val.size(), eat = lay.at.val.size();
+        size_t mm = std::max(m, 1), nn = std::max(n, 1);
+        size_t total = rounded(std::max<size_t>(ea, 1) * 4) + rounded(std::max<size_t>(eat, 1) * 4)
+                + 2 * rounded(mm * 4) + 6 * rounded(nn * 4) + 9 * rounded(nn * 4)
+                + 6 * rounded(mm * 4);
+        cudaError_t e = cudaMallocAsync(&mem32, total, stream);
+        if (e != cudaSuccess) {
+                mem32 = nullptr;
+                set_error(ACDALM_ENOMEM, "cudaMalloc(%zu bytes) for the FP32 copies: %s",
+                          total, cudaGetErrorString(e));
+                return ACDALM_ENOMEM;
+        }
+        bytes32 = total;
+        char * p = static_cast<char *>(mem32);
+        a_valf = carve<float>(p, std::max<size_t>(ea, 1));
+        at_valf = carve<float>(p, std::max<size_t>(eat, 1));
+        bf = carve<float>(p, mm);
+        wf = carve<float>(p, mm);
+        cf = carve<float>(p, nn);
+        lf = carve<float>(p, nn);
+        uf = carve<float>(p, nn);
+        vf = carve<float>(p, nn);
+        ivf = carve<float>(p, nn);
+        d = carve<float>(p, nn);
+        for (auto & q : wnf)
+                q = carve<float>(p, nn);
+        for (auto & q : wmf)
+                q = carve<float>(p, mm);
+        ACD_CUDA_TRY(cudaMemsetAsync(mem32, 0, total, stream), ACDALM_ECUDA);
+        std::vector<float> tmp(lay.a.val.begin(), lay.a.val.end());
+        if (ea)
+                ACD_CUDA_TRY(cudaMemcpyAsync(a_valf, tmp.data(), ea * 4, cudaMemcpyHostToDevice,
+                                             stream), ACDALM_ECUDA);
+        ACD_CUDA_TRY(cudaStreamSynchronize(stream), ACDALM_ECUDA);
+        tmp.assign(lay.at.val.begin(), lay.at.val.end());
+        if (eat)
+                ACD_CUDA_TRY(cudaMemcpyAsync(at_valf, tmp.data(), eat * 4, cudaMemcpyHostToDevice,
+                                             stream), ACDALM_ECUDA);
+        ACD_CUDA_TRY(cudaStreamSynchronize(stream), ACDALM_ECUDA);
+        return 0;
+}
+
 void DevInstance::destroy()
 {
+        if (mem32)
+                cudaFreeAsync(mem32, stream);
+        mem32 = nullptr;
         if (mem)
-                cudaFree(mem);
+                cudaFreeAsync(mem, stream);
         mem = nullptr;
         if (stream)
                 cudaStreamDestroy(stream);
@@ -609,10 +678,28 @@ int dev_step_sizes(DevInstance & d, const HostVectors & hv, double * beta_out,
         return 0;
 }
 
-int run_alm(DevInstance & d, const HostVectors & hv, size_t niter, double * x,
-            double * lam, FILE * log, double * diag3, const AlmSettings & s,
-            double * w_out, double * c_out, SolveStats & st)
+static double env_or(const char * name, double dflt)
 {
+        const char * e = getenv(name);
+        return e ? atof(e) : dflt;
+}
+
+// Uploads one instance's problem, x and lambda and fills the kernel
+// arguments of its ALM solve.
+static int alm_prepare(DevInstance & d, const HostVectors & hv, size_t niter, double * x,
+                       double * lam, bool want_log, const AlmSettings & s,
+                       const DeviceLayout * lay, AlmKernelArgs & k)
+{
+        bool mixed = s.precision == 1;
+        if (mixed) {
+                if (!lay) {
+                        set_error(ACDALM_EINVAL, "mixed precision needs the device layout");
+                        return ACDALM_EINVAL;
+                }
+                int e = d.ensure_f32(*lay);
+                if (e)
+                        return e;
+        }
         int r = upload_problem(d, hv);
         if (r)
                 return r;
@@ -626,7 +713,6 @@ int run_alm(DevInstance & d, const HostVectors & hv, size_t niter, double * x,
         if (hv.c0)
                 for (int j = 0; j < d.n; j++)
                         cn += hv.c0[j] * hv.c0[j];
-        AlmKernelArgs k;
         memset(&k, 0, sizeof(k));
         k.P.m = d.m;
         k.P.n = d.n;
@@ -652,35 +738,62 @@ int run_alm(DevInstance & d, const HostVectors & hv, size_t niter, double * x,
         k.a.niter = (long long)std::min<size_t>(niter, (size_t)1 << 62);
         k.a.inner_budget = s.inner_budget;
         k.a.kkt_tol = s.kkt_tol;
-        k.a.log = (log != nullptr);
+        k.a.log = want_log;
         k.a.limit_ns = solve_limit_ns();
+        k.a.mixed = mixed ? 1 : 0;
+        k.a.min_delta32 = env_or("ACDALM_MIN_DELTA32", 1e-6);
+        k.a.niter32 = (long long)env_or("ACDALM_NITER32", 200000);
+        k.a.stall_switch = (int)env_or("ACDALM_STALL_SWITCH", 3);
+        if (mixed) {
+                k.M.Af = {d.m, d.a_nslices, d.a_ptr, d.a_row0, d.a_col, d.a_valf};
+                k.M.Atf = {d.n, d.at_nslices, d.at_ptr, d.at_row0, d.at_col, d.at_valf};
+                k.M.bf = d.bf;
+                k.M.wf = d.wf;
+                k.M.cf = d.cf;
+                k.M.lf = d.lf;
+                k.M.uf = d.uf;
+                k.M.vf = d.vf;
+                k.M.ivf = d.ivf;
+                k.M.d = d.d;
+                InnerWork<float> Wf;
+                Wf.zx = d.wnf[0];
+                Wf.zpx = d.wnf[1];
+                Wf.xx = d.wnf[2];
+                Wf.g = d.wnf[3];
+                Wf.g2 = d.wnf[4];
+                Wf.prev = d.wnf[5];
+                Wf.prev_alt = d.wnf[6];
+                Wf.alt_x = d.wnf[7];
+                Wf.ux = d.wnf[8];
+                Wf.yv = d.wmf[0];
+                Wf.zv = d.wmf[1];
+                Wf.zpv = d.wmf[2];
+                Wf.xv = d.wmf[3];
+                Wf.alt_xv = d.wmf[4];
+                Wf.alt_yv = d.wmf[5];
+                k.M.Wf = Wf;
+        }
         k.x = d.x;
         k.lam = d.lam;
         k.ctl = static_cast<TeamCtl *>(d.ctl);
         k.slots = d.slots;
         k.result = d.result;
         k.out = static_cast<AlmOut *>(d.out);
-        cudaEvent_t e0, e1;
-        cudaEventCreate(&e0);
-        cudaEventCreate(&e1);
-        cudaEventRecord(e0, d.stream);
-        const void * fn = g_exact ? (const void *)alm_kernel<true>
-                                  : (const void *)alm_kernel<false>;
-        if ((r = launch_coop(fn, d.grid_blocks, &k, d.stream)))
-                return r;
-        cudaEventRecord(e1, d.stream);
-        ACD_CUDA_TRY(cudaStreamSynchronize(d.stream), ACDALM_ECUDA);
-        float ms = 0;
-        cudaEventElapsedTime(&ms, e0, e1);
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        int status = 0;
+        return 0;
+}
+
+// Reads one instance's outcome after its ALM kernel finished.
+static int alm_finish(DevInstance & d, const AlmKernelArgs & k, double * x, double * lam,
+                      FILE * log, double * diag3, double * w_out, double * c_out,
+                      SolveStats & st, double seconds)
+{
+        int status = 0, r;
         if ((r = read_status(d, status)))
                 return r;
         AlmOut out;
         ACD_CUDA_TRY(cudaMemcpy(&out, d.out, sizeof(out), cudaMemcpyDeviceToHost), ACDALM_ECUDA);
         fetch_logs(d, log);
-        st.seconds = ms * 1e-3;
+        st.seconds = seconds;
         st.inner = out.inner;
         st.outer = (unsigned long long)out.outer;
         st.rel_kkt = out.rel_kkt;
@@ -689,7 +802,8 @@ int run_alm(DevInstance & d, const HostVectors & hv, size_t niter, double * x,
         st.gap = out.gap;
         st.objective = out.objective;
         st.status = status;
-        st.precision = 0;
+        st.precision = k.a.mixed;
+        st.inner_fp32 = out.inner32;
         if (status != 0) {
                 set_error(status, "device solve failed with status %d%s", status,
                           status == ACDALM_ETIMEOUT ? " (a device wait timed out)"
@@ -709,6 +823,193 @@ int run_alm(DevInstance & d, const HostVectors & hv, size_t niter, double * x,
                 diag3[2] = out.diag[2];
         }
         return out.ret;
+}
+
+int run_alm(DevInstance & d, const HostVectors & hv, size_t niter, double * x,
+            double * lam, FILE * log, double * diag3, const AlmSettings & s,
+            double * w_out, double * c_out, SolveStats & st, const DeviceLayout * lay)
+{
+        AlmKernelArgs k;
+        int r = alm_prepare(d, hv, niter, x, lam, log != nullptr, s, lay, k);
+        if (r)
+                return r;
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, d.stream);
+        const void * fn = g_exact ? (const void *)alm_kernel<true>
+                                  : (const void *)alm_kernel<false>;
+        if ((r = launch_coop(fn, d.grid_blocks, &k, d.stream)))
+                return r;
+        cudaEventRecord(e1, d.stream);
+        ACD_CUDA_TRY(cudaStreamSynchronize(d.stream), ACDALM_ECUDA);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return alm_finish(d, k, x, lam, log, diag3, w_out, c_out, st, ms * 1e-3);
+}
+
+// ---- batches: one LP per CTA ---------------------------------------------
+
+namespace {
+
+constexpr int kBatchThreads = 256;
+
+// One LP on one CTA, its arguments passed by value (the server's launches).
+template <bool Exact>
+__global__ void __launch_bounds__(kBatchThreads, 2) alm_single_kernel(AlmKernelArgs k)
+{
+        BlockTeam tm{reinterpret_cast<int *>(&k.ctl->status_w.v)};
+        Alm<BlockTeam, Exact> alm(tm, k.P, k.W, k.log, k.M);
+        AlmOut out;
+        memset(&out, 0, sizeof(out));
+        int r = alm.solve(k.a, k.x, k.lam, out);
+        if (threadIdx.x == 0) {
+                if (r < 0)
+                        out.ret = r;
+                *k.out = out;
+        }
+}
+
+// Persistent CTAs take LPs from a shared counter (largest first) and run
+// each one's whole ALM solve with a one-CTA team.
+template <bool Exact>
+__global__ void __launch_bounds__(kBatchThreads, 2)
+alm_batch_kernel(const AlmKernelArgs * items, int count, int * next)
+{
+        __shared__ int cur;
+        for (;;) {
+                if (threadIdx.x == 0)
+                        cur = atomicAdd(next, 1);
+                __syncthreads();
+                int i = cur;
+                __syncthreads();
+                if (i >= count)
+                        break;
+                const AlmKernelArgs & k = items[i];
+                BlockTeam tm{reinterpret_cast<int *>(&k.ctl->status_w.v)};
+                Alm<BlockTeam, Exact> alm(tm, k.P, k.W, k.log, k.M);
+                AlmOut out;
+                memset(&out, 0, sizeof(out));
+                int r = alm.solve(k.a, k.x, k.lam, out);
+                if (threadIdx.x == 0) {
+                        if (r < 0)
+                                out.ret = r;
+                        *k.out = out;
+                }
+                __syncthreads();
+        }
+}
+
+}  // namespace
+
+struct AlmLaunch::Impl {
+        AlmKernelArgs k;
+};
+
+AlmLaunch::AlmLaunch() : impl(new Impl) {}
+AlmLaunch::~AlmLaunch()
+{
+        if (done)
+                cudaEventDestroy(done);
+        delete impl;
+}
+
+int alm_launch_async(DevInstance & d, const HostVectors & hv, size_t niter, double * x,
+                     double * lam, const AlmSettings & s, const DeviceLayout * lay,
+                     AlmLaunch & h)
+{
+        int r = alm_prepare(d, hv, niter, x, lam, false, s, lay, h.impl->k);
+        if (r)
+                return r;
+        if (!h.done)
+                ACD_CUDA_TRY(cudaEventCreateWithFlags(&h.done, cudaEventDisableTiming),
+                             ACDALM_ECUDA);
+        if (g_exact)
+                alm_single_kernel<true><<<1, kBatchThreads, 0, d.stream>>>(h.impl->k);
+        else
+                alm_single_kernel<false><<<1, kBatchThreads, 0, d.stream>>>(h.impl->k);
+        count_launch();
+        ACD_CUDA_TRY(cudaGetLastError(), ACDALM_ECUDA);
+        ACD_CUDA_TRY(cudaEventRecord(h.done, d.stream), ACDALM_ECUDA);
+        return 0;
+}
+
+int alm_collect(DevInstance & d, AlmLaunch & h, double * x, double * lam, double * diag3,
+                SolveStats & st)
+{
+        ACD_CUDA_TRY(cudaEventSynchronize(h.done), ACDALM_ECUDA);
+        return alm_finish(d, h.impl->k, x, lam, nullptr, diag3, nullptr, nullptr, st, 0);
+}
+
+int run_alm_batch(std::vector<BatchEntry> & entries, size_t niter, double * seconds)
+{
+        int count = (int)entries.size();
+        if (count == 0)
+                return 0;
+        std::vector<AlmKernelArgs> items(count);
+        int r;
+        for (int i = 0; i < count; i++) {
+                BatchEntry & e = entries[i];
+                if ((r = alm_prepare(*e.dev, e.hv, niter, e.x, e.lam, false, e.settings, e.lay,
+                                     items[i])))
+                        return r;
+        }
+        // largest LPs first: the persistent CTAs then balance the tail
+        std::vector<int> order(count);
+        for (int i = 0; i < count; i++)
+                order[i] = i;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+                return entries[a].dev->nnz > entries[b].dev->nnz;
+        });
+        std::vector<AlmKernelArgs> sorted(count);
+        for (int i = 0; i < count; i++)
+                sorted[i] = items[order[i]];
+        cudaStream_t s = entries[0].dev->stream;
+        void * mem = nullptr;
+        size_t bytes = sizeof(AlmKernelArgs) * count + 256;
+        ACD_CUDA_TRY(cudaMallocAsync(&mem, bytes, s), ACDALM_ENOMEM);
+        AlmKernelArgs * ditems = static_cast<AlmKernelArgs *>(mem);
+        int * next = reinterpret_cast<int *>(static_cast<char *>(mem) + sizeof(AlmKernelArgs) * count);
+        ACD_CUDA_TRY(cudaMemcpyAsync(ditems, sorted.data(), sizeof(AlmKernelArgs) * count,
+                                     cudaMemcpyHostToDevice, s), ACDALM_ECUDA);
+        ACD_CUDA_TRY(cudaMemsetAsync(next, 0, sizeof(int), s), ACDALM_ECUDA);
+        const void * fn = g_exact ? (const void *)alm_batch_kernel<true>
+                                  : (const void *)alm_batch_kernel<false>;
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kBatchThreads, 0);
+        int blocks = std::max(1, std::min(count, sms * std::max(per_sm, 1)));
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, s);
+        if (g_exact)
+                alm_batch_kernel<true><<<blocks, kBatchThreads, 0, s>>>(ditems, count, next);
+        else
+                alm_batch_kernel<false><<<blocks, kBatchThreads, 0, s>>>(ditems, count, next);
+        count_launch();
+        ACD_CUDA_TRY(cudaGetLastError(), ACDALM_ECUDA);
+        cudaEventRecord(e1, s);
+        ACD_CUDA_TRY(cudaStreamSynchronize(s), ACDALM_ECUDA);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaFreeAsync(mem, s);
+        if (seconds)
+                *seconds = ms * 1e-3;
+        int worst = 0;
+        for (int i = 0; i < count; i++) {
+                BatchEntry & e = entries[i];
+                e.ret = alm_finish(*e.dev, items[i], e.x, e.lam, nullptr, e.diag3, e.w_out,
+                                   e.c_out, *e.stats, ms * 1e-3);
+                if (e.ret < 0 && worst == 0)
+                        worst = e.ret;
+        }
+        return worst;
 }
 
 static int run_inner(DevInstance & d, const HostVectors & hv, double * x,

@@ -61,6 +61,9 @@ struct InnerArgs {
         int log;         // record log lines
         unsigned long long t_start_ns;  // globaltimer at the solve's start
         unsigned long long limit_ns;    // give up (ACDALM_ETIMEOUT) after this
+        // When the iterate is a correction d to a point xbar (the mixed
+        // precision mode), |xbar + d| is the norm the min_delta test uses.
+        const double * xbar;
 };
 
 template <class T>
@@ -135,6 +138,7 @@ struct Approx {
         int restarts_since_log;
         bool ok;
         unsigned long long t_start_ns;
+        const double * xbar = nullptr;
 
         __device__ Approx(Team & t, const InnerProblem<T> & p,
                           const InnerWork<T> & w, const LogBuf & lb)
@@ -175,8 +179,8 @@ struct Approx {
                 const T * xvr = x.viol;
                 const T * xxr = x.x;
                 sell_rows_1<Exact>(tm, P.A, v.x, [&](int i, T ax) {
-                        T r = ax - P.b[i];
-                        T s = mul<Exact>(P.w[i], r);
+                        T r = ax - tm.ld(P.b + i);
+                        T s = mul<Exact>(tm.ld(P.w + i), r);
                         v.viol[i] = s;
                         part[0] += (double)s * (double)r;
                         if (linterp) {
@@ -191,10 +195,11 @@ struct Approx {
                                 if (linterp)
                                         xxw[j] = lerp2<Exact>(ts, tm.ld(xxr + j), tt, vj);
                                 if (want_cx)
-                                        part[1] += (double)P.c[j] * (double)vj;
+                                        part[1] += (double)tm.ld(P.c + j) * (double)vj;
                                 if (want_delta) {
                                         double d = (double)tm.ld(W.prev + j) - (double)vj;
-                                        part[2] += (double)vj * (double)vj;
+                                        double full = xbar ? xbar[j] + (double)vj : (double)vj;
+                                        part[2] += full * full;
                                         part[3] += d * d;
                                 }
                         }
@@ -237,7 +242,7 @@ struct Approx {
                 T * g = W.g;
                 T * g2 = W.g2;
                 auto epi = [&](int j, T g0, T g1) {
-                        T cj = P.c[j];
+                        T cj = tm.ld(P.c + j);
                         if (two)
                                 g0 = g0 + cj;
                         g1 = g1 + cj;
@@ -245,8 +250,8 @@ struct Approx {
                                 g[j] = g0;
                         g2[j] = g1;
                         T zj = tm.ld(z.x + j);
-                        T lj = P.l[j], uj = P.u[j];
-                        T stp = mul<Exact>(it, P.inv_v[j]);
+                        T lj = tm.ld(P.l + j), uj = tm.ld(P.u + j);
+                        T stp = mul<Exact>(it, tm.ld(P.inv_v + j));
                         T trial = msub<Exact>(zj, g1, stp);
                         trial = maxpd(lj, trial);
                         trial = minpd(uj, trial);
@@ -255,7 +260,7 @@ struct Approx {
                         if (is_long) {
                                 part[0] += (double)g1 * (double)delta;
                                 part[1] += (double)delta * (double)delta
-                                        * (double)t2 * (double)P.v[j];
+                                        * (double)t2 * (double)tm.ld(P.v + j);
                         } else {
                                 double a = fabs((double)trial);
                                 part[0] = (a > part[0]) ? a : part[0];
@@ -299,12 +304,12 @@ struct Approx {
                 const int op[2] = {RED_SUM, RED_SUM};
                 T * g = W.g;
                 sell_rows_1<Exact>(tm, P.At, v.viol, [&](int j, T a) {
-                        T gj = a + P.c[j];
+                        T gj = a + tm.ld(P.c + j);
                         g[j] = gj;
                         T xj = tm.ld(v.x + j);
                         T xp = xj - gj;
-                        xp = maxpd(P.l[j], xp);
-                        xp = minpd(P.u[j], xp);
+                        xp = maxpd(tm.ld(P.l + j), xp);
+                        xp = minpd(tm.ld(P.u + j), xp);
                         double d = (double)xj - (double)xp;
                         part[0] += d * d;
                         part[1] += (double)gj * (double)gj;
@@ -330,16 +335,16 @@ struct Approx {
                 T * g = W.g;
                 auto body = [&](int j, T gj) {
                         T zj = tm.ld(z.x + j);
-                        T stp = mul<Exact>(it, P.inv_v[j]);
+                        T stp = mul<Exact>(it, tm.ld(P.inv_v + j));
                         T trial = msub<Exact>(zj, tm.ld(W.g2 + j), stp);
-                        trial = maxpd(P.l[j], trial);
-                        trial = minpd(P.u[j], trial);
+                        trial = maxpd(tm.ld(P.l + j), trial);
+                        trial = minpd(tm.ld(P.u + j), trial);
                         zp.x[j] = trial;
                         part[0] += (double)gj * ((double)trial - (double)zj);
                 };
                 if (need_grad) {
                         sell_rows_1<Exact>(tm, P.At, z.viol, [&](int j, T a) {
-                                T gj = a + P.c[j];
+                                T gj = a + tm.ld(P.c + j);
                                 g[j] = gj;
                                 body(j, gj);
                         });
@@ -385,7 +390,7 @@ struct Approx {
                         double part[1] = {0};
                         const int op[1] = {RED_SUM};
                         for (int j = tm.tid(); j < P.n; j += tm.nthreads())
-                                part[0] += (double)P.c[j] * (double)tm.ld(v.x + j);
+                                part[0] += (double)tm.ld(P.c + j) * (double)tm.ld(v.x + j);
                         if (!tm.reduce(part, op))
                                 return false;
                         cx = part[0];
@@ -402,7 +407,8 @@ struct Approx {
                 for (int j = tm.tid(); j < P.n; j += tm.nthreads()) {
                         double vj = (double)tm.ld(v.x + j);
                         double d = (double)tm.ld(W.prev + j) - vj;
-                        part[0] += vj * vj;
+                        double full = xbar ? xbar[j] + vj : vj;
+                        part[0] += full * full;
                         part[1] += d * d;
                 }
                 if (!tm.reduce(part, op))
@@ -556,6 +562,7 @@ struct Approx {
                              long long * iters_out)
         {
                 t_start_ns = a.t_start_ns;
+                xbar = a.xbar;
                 // state init (approx.c:588-603)
                 y = {nullptr, W.yv, 0, NAN, NAN};
                 z = {W.zx, W.zv, 0, NAN, NAN};
@@ -567,8 +574,8 @@ struct Approx {
                 restarts_since_log = 0;
                 for (int j = tm.tid(); j < P.n; j += tm.nthreads()) {
                         T xj = tm.ld(x_io + j);
-                        T lo = maxpd(P.l[j], xj);
-                        x.x[j] = minpd(lo, P.u[j]);
+                        T lo = maxpd(tm.ld(P.l + j), xj);
+                        x.x[j] = minpd(lo, tm.ld(P.u + j));
                 }
                 if (!tm.sync())
                         return -1;
@@ -733,6 +740,21 @@ struct AlmArgs {
         double kkt_tol;                   // 0 = off
         int log;
         unsigned long long limit_ns;      // whole-solve time limit (0 = none)
+        // mixed precision (FP32 inner iterations on the correction to an
+        // FP64 point, FP64 everywhere else)
+        int mixed;
+        double min_delta32;               // the FP32 inner solves' stall test
+        long long niter32;                // cap per FP32 inner solve
+        int stall_switch;                 // FP32 stalls in a row before the
+                                          // remaining outer iterations run FP64
+};
+
+// The FP32 copies the mixed mode works on (device order).
+struct AlmMixed {
+        SellDev<float> Af, Atf;
+        float * bf, * wf;                              // m
+        float * cf, * lf, * uf, * vf, * ivf, * d;      // n
+        InnerWork<float> Wf;
 };
 
 struct AlmOut {
@@ -740,6 +762,7 @@ struct AlmOut {
         double diag[3];          // objective, max violation, pg
         long long outer;
         unsigned long long inner;
+        unsigned long long inner32;  // of which FP32 (mixed mode)
         double primal, dual, gap, rel_kkt, objective;
 };
 
@@ -749,10 +772,11 @@ struct Alm {
         AlmProblem P;
         InnerWork<double> W;
         LogBuf log;
+        AlmMixed mixed;
 
         __device__ Alm(Team & t, const AlmProblem & p, const InnerWork<double> & w,
-                       const LogBuf & lb)
-                : tm(t), P(p), W(w), log(lb) {}
+                       const LogBuf & lb, const AlmMixed & mxd)
+                : tm(t), P(p), W(w), log(lb), mixed(mxd) {}
 
         // penalise_linear (alm.c:106-119) + approx_update_step_size of the
         // permuted instance (approx.c:135-186) in one pass over A':
@@ -761,7 +785,8 @@ struct Alm {
         // where v = 0 and c = 0).  Partials: lambda'b, and the relative KKT
         // terms of (x, lambda) when kkt is set.
         __device__ bool penalise(const double * lam, const double * x, bool kkt,
-                                 double (&out)[6], bool write = true)
+                                 double (&out)[6], bool write = true,
+                                 const AlmMixed * mx = nullptr)
         {
                 double part[6] = {0, 0, 0, 0, 0, 0};
                 const int op[6] = {RED_SUM, RED_SUM, RED_SUM, RED_SUM, RED_SUM, RED_SUM};
@@ -790,9 +815,22 @@ struct Alm {
                         if (sl.lead && j < P.n) {
                                 double cj = P.c0[j] - acc;
                                 if (write) {
+                                        double ivj = (vv == 0 && cj == 0) ? 1.0 : 1.0 / vv;
                                         P.c[j] = cj;
                                         P.v[j] = vv;
-                                        P.inv_v[j] = (vv == 0 && cj == 0) ? 1.0 : 1.0 / vv;
+                                        P.inv_v[j] = ivj;
+                                        if (mx) {
+                                                // the FP32 inner problem in the
+                                                // correction d = x - xbar
+                                                double xj = tm.ld(x + j);
+                                                mx->cf[j] = (float)cj;
+                                                mx->vf[j] = (float)vv;
+                                                mx->ivf[j] = (float)ivj;
+                                                mx->lf[j] = (float)(P.l[j] - xj);
+                                                mx->uf[j] = (float)(P.u[j] - xj);
+                                                mx->d[j] = 0.f;
+                                                part[5] += cj * xj;
+                                        }
                                 }
                                 if (kkt) {
                                         double xj = tm.ld(x + j);
@@ -814,6 +852,10 @@ struct Alm {
                         if (kkt) {
                                 double ri = tm.ld(P.r + i);
                                 part[4] += ri * ri;
+                        }
+                        if (mx && write) {
+                                mx->bf[i] = (float)(-tm.ld(P.r + i));
+                                mx->wf[i] = (float)tm.ld(P.w + i);
                         }
                 }
                 if (!tm.reduce(part, op))
@@ -908,6 +950,23 @@ struct Alm {
                 }
         }
 
+        // r = A x - b (FP64), without touching the multipliers.
+        __device__ bool residual(const double * x)
+        {
+                sell_rows_1<Exact>(tm, P.A, x, [&](int i, double ax) { P.r[i] = ax - P.b[i]; });
+                return tm.sync();
+        }
+
+        // x <- P[l,u](x + d) in FP64 after an FP32 inner solve on d.
+        __device__ bool apply_correction(double * x, const float * d)
+        {
+                for (int j = tm.tid(); j < P.n; j += tm.nthreads()) {
+                        double v = tm.ld(x + j) + (double)tm.ld(d + j);
+                        x[j] = fmax(P.l[j], fmin(v, P.u[j]));
+                }
+                return tm.sync();
+        }
+
         // alm_solve, alm.c:289-322; x (n) and lam (m) in device order.
         __device__ int solve(const AlmArgs & a, double * x, double * lam, AlmOut & out)
         {
@@ -935,8 +994,29 @@ struct Alm {
                 ip.u = P.u;
                 ip.v = P.v;
                 ip.inv_v = P.inv_v;
+                const AlmMixed * mx = a.mixed ? &mixed : nullptr;
+                bool fp64_inner = false;
+                int stalls = 0;
+                unsigned long long inner32 = 0;
+                InnerProblem<float> ipf;
+                if (mx) {
+                        ipf.m = P.m;
+                        ipf.n = P.n;
+                        ipf.A = mixed.Af;
+                        ipf.At = mixed.Atf;
+                        ipf.b = mixed.bf;
+                        ipf.w = mixed.wf;
+                        ipf.c = mixed.cf;
+                        ipf.l = mixed.lf;
+                        ipf.u = mixed.uf;
+                        ipf.v = mixed.vf;
+                        ipf.inv_v = mixed.ivf;
+                        if (!residual(x))
+                                return -1;
+                }
                 for (k = 0; k < a.niter; k++) {
-                        if (!penalise(lam, x, kkt && k > 0, kk))
+                        if (!penalise(lam, x, kkt && k > 0, kk, true,
+                                      (mx && !fp64_inner) ? mx : nullptr))
                                 return -1;
                         if (kkt && k > 0) {
                                 double primal = sqrt(kk[4]) / (1 + P.bnorm);
@@ -970,12 +1050,36 @@ struct Alm {
                         ia.log = a.log;
                         ia.t_start_ns = t_start;
                         ia.limit_ns = a.limit_ns;
-                        Approx<double, Team, Exact> ap(tm, ip, W, log);
+                        ia.xbar = nullptr;
                         double diag[5];
                         long long used = 0;
-                        int reason = ap.solve(ia, x, diag, &used);
-                        if (reason < 0)
-                                return -1;
+                        int reason;
+                        if (mx && !fp64_inner) {
+                                // FP32 iterations on the correction d to x:
+                                // same problem shifted by x, so the rounding
+                                // applies to d (iterative refinement)
+                                InnerArgs fa = ia;
+                                fa.offset = ia.offset + kk[5];
+                                fa.min_delta = fmax(ia.min_delta, a.min_delta32);
+                                if (a.niter32 > 0 && fa.niter > a.niter32)
+                                        fa.niter = a.niter32;
+                                fa.xbar = x;
+                                Approx<float, Team, Exact> apf(tm, ipf, mx->Wf, log);
+                                reason = apf.solve(fa, mx->d, diag, &used);
+                                if (reason < 0)
+                                        return -1;
+                                inner32 += (unsigned long long)used;
+                                if (!apply_correction(x, mx->d))
+                                        return -1;
+                                stalls = (reason == 2) ? 0 : stalls + 1;
+                                if (stalls >= a.stall_switch)
+                                        fp64_inner = true;
+                        } else {
+                                Approx<double, Team, Exact> ap(tm, ip, W, log);
+                                reason = ap.solve(ia, x, diag, &used);
+                                if (reason < 0)
+                                        return -1;
+                        }
                         inner_used += (unsigned long long)used;
                         double vo[4];
                         if (!violation(x, lam, vo))
@@ -1009,7 +1113,9 @@ struct Alm {
                         rec.a[5] = wsum / (double)P.m;
                         if (a.log)
                                 put_log(rec);
-                        if ((max_viol < 1e-5) && (stalled || pg < 1e-5)) {
+                        // the reference's stop (alm.c:306-308); a relative
+                        // KKT tolerance, when set, is the stop instead
+                        if (!kkt && (max_viol < 1e-5) && (stalled || pg < 1e-5)) {
                                 ret = 0;
                                 k++;
                                 break;
@@ -1040,6 +1146,7 @@ struct Alm {
                 out.diag[2] = pg;
                 out.outer = k;
                 out.inner = inner_used;
+                out.inner32 = inner32;
                 return ret;
         }
 };

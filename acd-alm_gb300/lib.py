@@ -107,6 +107,25 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.acdalm_approx_permuted_matrix.restype = _vp
     L.acdalm_approx_permuted_matrix.argtypes = [_vp]
     L.acdalm_approx_step_sizes.argtypes = [_vp, _f64p, _f64p, _f64p]
+    L.acdalm_batch_make.restype = _vp
+    L.acdalm_batch_make.argtypes = [_vp, _sz]
+    L.acdalm_batch_solve.argtypes = [_vp, _sz, _vp, _vp, _vp, _vp]
+    L.acdalm_batch_seconds.restype = C.c_double
+    L.acdalm_batch_seconds.argtypes = [_vp]
+    L.acdalm_batch_free.argtypes = [_vp]
+    L.acdalm_alm_approx.restype = _vp
+    L.acdalm_alm_approx.argtypes = [_vp]
+    L.acdalm_launch_count.restype = C.c_ulonglong
+    L.acdalm_set_rounding.argtypes = [C.c_int]
+    L.acdalm_server_create.restype = _vp
+    L.acdalm_server_create.argtypes = [_sz, C.c_int, C.c_int, C.c_double, C.c_int]
+    L.acdalm_server_submit.restype = C.c_longlong
+    L.acdalm_server_submit.argtypes = [_vp, _sz, _sz, _sz, _u32p, _u32p, _f64p, _f64p, _vp,
+                                       _vp, _vp, _vp, _vp]
+    L.acdalm_server_poll.argtypes = [_vp, _vp, C.c_int, C.c_double]
+    L.acdalm_server_result.argtypes = [_vp, C.c_longlong, _vp, _vp, C.POINTER(Stats),
+                                       C.POINTER(C.c_double)]
+    L.acdalm_server_destroy.argtypes = [_vp]
     L.thread_pool_init.restype = _vp
     L.thread_pool_init.argtypes = [C.c_uint]
     L.thread_pool_free.argtypes = [_vp]
@@ -349,3 +368,81 @@ def _open_log(path):
 def _close_log(f):
     if f:
         _libc.fclose(f)
+
+
+class Batch:
+    """acdalm_batch_t: alm_solve on many Alm instances in one launch."""
+
+    def __init__(self, alms):
+        self.alms = list(alms)
+        arr = (_vp * max(len(self.alms), 1))(*[a.h for a in self.alms])
+        self.h = lib().acdalm_batch_make(arr, len(self.alms))
+        if not self.h:
+            raise AcdalmError(lib().acdalm_last_error().decode())
+
+    def solve(self, niter=1000, xs=None, lams=None):
+        n = len(self.alms)
+        xs = [np.zeros(a.ncols) if xs is None else np.ascontiguousarray(xs[i], np.float64).copy()
+              for i, a in enumerate(self.alms)]
+        lams = [np.zeros(a.nrows) if lams is None else np.ascontiguousarray(lams[i], np.float64).copy()
+                for i, a in enumerate(self.alms)]
+        DP = C.POINTER(C.c_double)
+        xa = (DP * max(n, 1))(*[x.ctypes.data_as(DP) for x in xs])
+        la = (DP * max(n, 1))(*[l.ctypes.data_as(DP) for l in lams])
+        ret = np.zeros(max(n, 1), np.int32)
+        diag = np.zeros(3 * max(n, 1))
+        r = lib().acdalm_batch_solve(self.h, niter, C.cast(xa, _vp), C.cast(la, _vp),
+                                     ret.ctypes.data_as(_vp), diag.ctypes.data_as(_vp))
+        check(r, "acdalm_batch_solve")
+        return ret[:n], xs, lams, diag[:3 * n].reshape(n, 3)
+
+    def seconds(self) -> float:
+        return lib().acdalm_batch_seconds(self.h)
+
+    def free(self):
+        if self.h:
+            lib().acdalm_batch_free(self.h)
+        self.h = None
+
+
+class Server:
+    """acdalm_server_t: continuous batching of LP solves."""
+
+    def __init__(self, device_budget=0, max_inflight=0, precision=PRECISION_MIXED,
+                 kkt_tol=1e-6, builder_threads=0):
+        self.h = lib().acdalm_server_create(device_budget, max_inflight, precision, kkt_tol,
+                                            builder_threads)
+        if not self.h:
+            raise AcdalmError(lib().acdalm_last_error().decode())
+        self.shapes = {}
+
+    def submit(self, lp) -> int:
+        keep = [np.ascontiguousarray(a, np.float64) for a in
+                (lp.linear, lp.lower, lp.upper, lp.lambda_lower, lp.lambda_upper)]
+        rid = lib().acdalm_server_submit(
+            self.h, lp.nrows, lp.ncols, lp.nnz, np.ascontiguousarray(lp.rows, np.uint32),
+            np.ascontiguousarray(lp.cols, np.uint32), np.ascontiguousarray(lp.vals, np.float64),
+            np.ascontiguousarray(lp.rhs, np.float64), *[_ptr(k) for k in keep])
+        check(rid, "acdalm_server_submit")
+        self.shapes[rid] = (lp.nrows, lp.ncols)
+        return rid
+
+    def poll(self, timeout=0.0, cap=1024):
+        ids = np.zeros(cap, np.int64)
+        n = lib().acdalm_server_poll(self.h, ids.ctypes.data_as(_vp), cap, timeout)
+        return [int(i) for i in ids[:n]]
+
+    def result(self, rid):
+        m, n = self.shapes.pop(rid)
+        x = np.zeros(n)
+        lam = np.zeros(m)
+        st = Stats()
+        lat = C.c_double()
+        r = lib().acdalm_server_result(self.h, rid, x.ctypes.data_as(_vp),
+                                       lam.ctypes.data_as(_vp), C.byref(st), C.byref(lat))
+        return r, x, lam, st.as_dict(), lat.value
+
+    def close(self):
+        if self.h:
+            lib().acdalm_server_destroy(self.h)
+        self.h = None

@@ -57,8 +57,10 @@ size_t acdalm_matrix_device_bytes(const struct sparse_matrix * a);
 #define ACDALM_PRECISION_MIXED 1 /* FP32 inner iterations, FP64 outer loop
                                     and final refinement */
 int alm_set_precision(struct alm *, int mode);
-/* Extra stop for alm_solve: the relative KKT residual (max of primal,
- * dual and gap terms, FP64) falls below tol (0 = off, the default). */
+/* Stop alm_solve when the relative KKT residual (max of the primal, dual
+ * and gap terms, FP64, checked after every outer iteration) is <= tol; it
+ * then replaces the reference's stop rule (largest violation < 1e-5 and
+ * projected gradient < 1e-5).  0 = off, the default. */
 int alm_set_kkt_tolerance(struct alm *, double tol);
 /* Cap on the total inner iterations of one alm_solve (0 = none). */
 int alm_set_inner_budget(struct alm *, uint64_t budget);
@@ -87,6 +89,61 @@ int acdalm_set_rounding(int exact);
 void * alm_stream(struct alm *);
 void * approx_stream(struct approx *);
 
+
+/* ---- batches: many independent LPs at once ---- */
+/* A batch borrows alm_t instances (made with alm_make, settings from
+ * alm_set_*).  acdalm_batch_solve runs alm_solve on every instance in one
+ * persistent launch: each LP runs on its own CTA, whose barriers are CTA
+ * barriers; CTAs take LPs from a shared counter, largest first, until all
+ * are done.  x[i] and lambda[i] are instance i's host arrays (in/out, as in
+ * alm_solve); ret[i] (may be NULL) its alm_solve return value; diag (may be
+ * NULL) 3 doubles per instance.  alm_last_stats(instances[i]) reports each
+ * instance.  Returns 0, or the first negative ACDALM_E* code. */
+typedef struct acdalm_batch acdalm_batch_t;
+acdalm_batch_t * acdalm_batch_make(struct alm * const * instances, size_t count);
+int acdalm_batch_solve(acdalm_batch_t * b, size_t niter, double * const * x,
+                       double * const * lambda, int * ret, double * diag);
+/* Device time of the last acdalm_batch_solve launch, seconds. */
+double acdalm_batch_seconds(acdalm_batch_t * b);
+int acdalm_batch_free(acdalm_batch_t * b);
+
+/* ---- serving: continuous batching ---- */
+/* A server accepts LPs at any time and solves them to a relative KKT
+ * residual <= kkt_tol (alm_solve with alm_set_kkt_tolerance; precision an
+ * ACDALM_PRECISION_* mode).  Builder threads (builder_threads, 0 = half
+ * the cores) prepare each LP's layouts in arrival order; requests are
+ * admitted, in arrival order, while their device footprint fits
+ * device_budget bytes (0 = 80% of the free memory) and fewer than
+ * max_inflight solves run (0 = 128).  Each admitted LP runs on one CTA of
+ * its own launch and stream, beside the others; a finished solve is retired
+ * and its memory returned.  The result of an LP does not depend on what
+ * else runs (one CTA, deterministic reductions). */
+typedef struct acdalm_server acdalm_server_t;
+acdalm_server_t * acdalm_server_create(size_t device_budget, int max_inflight,
+                                       int precision, double kkt_tol,
+                                       int builder_threads);
+/* Copies the LP (the arguments of sparse_matrix_make + alm_make; NULL
+ * vectors take alm_make's defaults) and queues it; returns its id (>= 0)
+ * or a negative code. */
+long long acdalm_server_submit(acdalm_server_t * s, size_t nrows, size_t ncols,
+                               size_t nnz, const uint32_t * rows,
+                               const uint32_t * cols, const double * values,
+                               const double * rhs, const double * linear,
+                               const double * lower, const double * upper,
+                               const double * lambda_lower,
+                               const double * lambda_upper);
+/* Waits up to timeout seconds for finished requests; writes up to cap ids
+ * and returns how many. */
+int acdalm_server_poll(acdalm_server_t * s, long long * ids, int cap, double timeout);
+/* Results of a finished request (then forgotten): x (ncols) and lambda
+ * (nrows) may be NULL; st the solve's statistics (seconds = admission to
+ * completion); *latency = submission to completion, seconds.  Returns the
+ * request's alm_solve value or a negative code. */
+int acdalm_server_result(acdalm_server_t * s, long long id, double * x,
+                         double * lambda, acdalm_stats_t * st, double * latency);
+/* Stops the server after the running solves finish; unfinished requests
+ * are dropped. */
+int acdalm_server_destroy(acdalm_server_t * s);
 
 /* ---- layout inspection (for parity checks against the reference) ---- */
 /* The 4-row block arena of A (transpose = 0) or A' (1), byte for byte the

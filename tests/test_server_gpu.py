@@ -1,0 +1,65 @@
+"""The LP server (acdalm_server_*): requests submitted while others run are
+admitted and solved beside them; every LP reaches a relative KKT residual
+<= 1e-6, and its result is bit-identical whether it was solved alone (a
+server holding only it) or in the mix of a busy server."""
+import time
+
+import numpy as np
+import pytest
+
+from libutil import binding
+
+pytestmark = pytest.mark.gpu
+
+
+def _lps(instances, count, seed):
+    rng = np.random.default_rng(seed)
+    sizes = np.floor(np.exp(rng.uniform(np.log(50), np.log(600), size=count))).astype(int)
+    return [instances.batch_instance(int(m), seed * 7919 + i) for i, m in enumerate(sizes)]
+
+
+def _serve(b, lps, gap=0.0, **kw):
+    srv = b.Server(**kw)
+    ids = []
+    for lp in lps:
+        ids.append(srv.submit(lp))
+        if gap:
+            time.sleep(gap)
+    out = {}
+    deadline = time.time() + 300
+    while len(out) < len(ids) and time.time() < deadline:
+        for rid in srv.poll(timeout=0.5):
+            out[rid] = srv.result(rid)
+    srv.close()
+    assert len(out) == len(ids)
+    return [out[i] for i in ids]
+
+
+def test_server_solves_every_request(instances):
+    b = binding()
+    lps = _lps(instances, 16, 3)
+    res = _serve(b, lps, gap=0.002, max_inflight=6)
+    for lp, (r, x, lam, st, lat) in zip(lps, res):
+        assert r == 0, st
+        k = instances.rel_kkt(lp, x, lam)
+        assert k["rel_kkt"] <= 1.01e-6, k
+        assert st["rel_kkt"] <= 1e-6
+        assert lat > 0
+
+
+def test_same_alone_and_in_the_mix(instances):
+    b = binding()
+    lps = _lps(instances, 12, 5)
+    mixed = _serve(b, lps, max_inflight=12)
+    for i in (0, 5, 11):
+        alone = _serve(b, [lps[i]], max_inflight=1)[0]
+        assert alone[1].tobytes() == mixed[i][1].tobytes(), i
+        assert alone[2].tobytes() == mixed[i][2].tobytes(), i
+
+
+def test_budget_admits_one_at_a_time(instances):
+    """A budget that fits one instance still serves them all, in order."""
+    b = binding()
+    lps = _lps(instances, 4, 9)
+    res = _serve(b, lps, device_budget=24 << 20, max_inflight=8)
+    assert all(r[0] == 0 for r in res)

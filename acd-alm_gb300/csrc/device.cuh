@@ -17,6 +17,7 @@
 // others records ACDALM_ETIMEOUT in the team's status word and every thread
 // returns; nothing traps.
 #pragma once
+#include <cooperative_groups.h>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -321,6 +322,74 @@ struct BlockTeam {
         __device__ bool sync()
         {
                 __syncthreads();
+                return true;
+        }
+};
+
+// The CTAs of one thread-block cluster (one large LP of a batch or a
+// server): barriers are the hardware cluster barrier (release / acquire at
+// cluster scope); each CTA publishes its partials in its own shared memory
+// and every CTA sums all CTAs' partials, read through distributed shared
+// memory, in rank order -- so every thread gets the same bits.
+struct ClusterTeam {
+        int * status;
+        unsigned rank, size;
+        int parity;
+
+        static constexpr bool kShared = false;
+
+        __device__ explicit ClusterTeam(int * st) : status(st), parity(0)
+        {
+                cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
+                rank = cl.block_rank();
+                size = cl.num_blocks();
+        }
+
+        __device__ int nthreads() const { return size * blockDim.x; }
+        __device__ int tid() const { return rank * blockDim.x + threadIdx.x; }
+        __device__ int warp() const { return tid() >> 5; }
+        __device__ int nwarps() const { return nthreads() >> 5; }
+        // data other CTAs of the cluster write: L2, not a possibly stale L1
+        template <class T>
+        __device__ __forceinline__ T ld(const T * p) const { return __ldcg(p); }
+        __device__ bool failed() const { return ld_acquire_int(status) != 0; }
+        __device__ void fail(int code) { atomicCAS(status, 0, code); }
+
+        // Failures are decided from reduced values, identically in every CTA,
+        // so the reduction needs no status check.
+        template <int K>
+        __device__ bool reduce(double (&v)[K], const int (&op)[K])
+        {
+                __shared__ double part[2][kRedMax];
+                __shared__ double tot[kRedMax];
+                block_reduce<K>(v, op, tot);
+                if (threadIdx.x < K)
+                        part[parity][threadIdx.x] = tot[threadIdx.x];
+                cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
+                cl.sync();
+                int lane = threadIdx.x & 31, wk = threadIdx.x >> 5;
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                        if (wk != k)
+                                continue;
+                        double val = red_identity(op[k]);
+                        if ((unsigned)lane < size)
+                                val = *cl.map_shared_rank(&part[parity][k], lane);
+                        val = warp_reduce(val, op[k]);
+                        if (lane == 0)
+                                tot[k] = val;
+                }
+                __syncthreads();
+#pragma unroll
+                for (int k = 0; k < K; k++)
+                        v[k] = tot[k];
+                parity ^= 1;
+                return true;
+        }
+
+        __device__ bool sync()
+        {
+                cooperative_groups::this_cluster().sync();
                 return true;
         }
 };

@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 
 #include "common.h"
 
@@ -45,10 +46,14 @@ int last_error_code()
         return t_code;
 }
 
+void preload_solver_kernels();
+void preload_spmv_kernels();
+
 bool device_ready()
 {
         static int count = -1;
         static int device = 0;
+        static bool loaded[64] = {};
         if (count < 0) {
                 if (cudaGetDeviceCount(&count) != cudaSuccess)
                         count = 0;
@@ -63,6 +68,15 @@ bool device_ready()
         if (cudaSetDevice(device) != cudaSuccess) {
                 set_error(ACDALM_ENODEV, "cudaSetDevice(%d) failed", device);
                 return false;
+        }
+        if (device < 64 && !loaded[device]) {
+                static std::mutex mu;
+                std::lock_guard<std::mutex> g(mu);
+                if (!loaded[device]) {
+                        preload_solver_kernels();
+                        preload_spmv_kernels();
+                        loaded[device] = true;
+                }
         }
         return true;
 }

@@ -140,9 +140,14 @@ struct AlmLaunch {
         AlmLaunch(const AlmLaunch &) = delete;
         AlmLaunch & operator=(const AlmLaunch &) = delete;
 };
+// team = CTAs working on the LP: 1 (one CTA) or a thread-block cluster of
+// 2..16 CTAs.
 int alm_launch_async(DevInstance & d, const HostVectors & hv, size_t niter, double * x,
                      double * lam, const AlmSettings & s, const DeviceLayout * lay,
-                     AlmLaunch & h);
+                     AlmLaunch & h, int team = 1);
+// The largest cluster (CTAs) the device can run one LP's solve on (16 when
+// the hardware allows it, else 8, 4, ...).
+int max_cluster_team();
 // After `done`: status, results (x, lambda in original order) and stats.
 int alm_collect(DevInstance & d, AlmLaunch & h, double * x, double * lam, double * diag3,
                 SolveStats & st);

@@ -271,11 +271,11 @@ std::vector<int32_t> order_by_length(const std::vector<uint32_t> & ptr)
 // Lanes per row for a slice whose longest row has `len` entries.
 int lanes_for(uint32_t len)
 {
-        if (len <= 32)
+        if (len <= 16)
                 return 1;
-        if (len <= 128)
+        if (len <= 64)
                 return 4;
-        if (len <= 512)
+        if (len <= 256)
                 return 16;
         return 32;
 }

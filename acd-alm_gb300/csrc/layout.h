@@ -59,7 +59,7 @@ void ensure_zorder(HostMatrix & m);
 // Warp-sliced ELL of one operator (A or A') in device order, with a
 // per-slice height.  A slice is 32 lanes wide; it holds h = 32 / L
 // consecutive rows, each row spread over L lanes (L = 1, 4, 16 or 32, chosen
-// from the slice's longest row so no slice needs more than ~32 steps).
+// from the slice's longest row so no slice needs more than ~16 steps).
 // Element k of the slice's r-th row sits at step k / L, lane r * L + k % L,
 // i.e. at offset ptr + 32 * (k / L) + r * L + k % L.  ptr is a multiple of
 // 32; its low 5 bits hold log2(L).

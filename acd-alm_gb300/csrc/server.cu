@@ -5,17 +5,19 @@
 // device layout) in arrival order.  A dispatcher thread admits built
 // requests while their device footprint fits the memory budget and fewer
 // than max_inflight solves run: each admitted LP gets its device instance,
-// its data uploaded, and one single-CTA solve launched on its own stream,
-// so LPs that arrive while others are on the GPU run beside them.  Finished
+// its data uploaded, and one solve launched on its own stream -- one CTA for
+// a small LP, a thread-block cluster of up to 16 CTAs for a large one -- so
+// LPs that arrive while others are on the GPU run beside them.  Finished
 // solves are retired (results read back, device memory freed), which frees
 // budget for the next requests.  Every solve is the same computation whether
-// it runs alone or in the mix (one CTA, deterministic reductions).
+// it runs alone or in the mix (a fixed team, deterministic reductions).
 #include <cuda_runtime.h>
 
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
+#include <algorithm>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -47,6 +49,7 @@ struct Request {
         sparse_matrix_t * matrix = nullptr;
         alm_t * alm = nullptr;
         size_t footprint = 0;
+        int team = 1;  // CTAs (a thread-block cluster) solving this LP
         acd::AlmLaunch launch;
         std::vector<double> x, lam;
         double diag[3] = {0, 0, 0};
@@ -60,6 +63,7 @@ struct Request {
 
 struct acdalm_server {
         size_t budget = 0;         // device bytes for admitted instances
+        int max_team = 16;         // largest cluster the device launches
         size_t in_use = 0;
         int max_inflight = 0;
         int precision = 0;
@@ -84,6 +88,18 @@ struct acdalm_server {
 
 namespace {
 
+// Cluster size (CTAs per LP) for an LP with nnz nonzeros.
+int team_size(long long nnz)
+{
+        if (nnz <= 150000)
+                return 1;
+        if (nnz <= 600000)
+                return 4;
+        if (nnz <= 1500000)
+                return 8;
+        return 16;
+}
+
 void build_one(acdalm_server_t * s, Request * r)
 {
         r->matrix = sparse_matrix_make(r->n, r->m, r->vals.size(), r->rows.data(),
@@ -92,6 +108,16 @@ void build_one(acdalm_server_t * s, Request * r)
                 r->alm = alm_make(r->matrix, r->m, r->rhs.data(), r->n, r->linear.data(),
                                   r->lower.data(), r->upper.data(), r->llo.data(),
                                   r->lhi.data());
+        if (r->alm) {
+                approx_t * a = r->alm->approx;
+                acd::build_device_layout(acd::host_of(a->permuted), a->lay);
+                a->lay_ready = true;
+                r->team = std::min(team_size((long long)r->vals.size()), s->max_team);
+                // the COO copies are not needed any more
+                std::vector<uint32_t>().swap(r->rows);
+                std::vector<uint32_t>().swap(r->cols);
+                std::vector<double>().swap(r->vals);
+        }
         std::lock_guard<std::mutex> g(s->mu);
         if (!r->alm) {
                 r->state = FAILED;
@@ -102,16 +128,10 @@ void build_one(acdalm_server_t * s, Request * r)
                 return;
         }
         approx_t * a = r->alm->approx;
-        acd::build_device_layout(acd::host_of(a->permuted), a->lay);
-        a->lay_ready = true;
         r->alm->settings.kkt_tol = s->kkt_tol;
         r->alm->settings.precision = s->precision;
         r->alm->settings.inner_budget = s->inner_budget;
         r->footprint = acd::DevInstance::footprint(a->lay, s->precision == 1);
-        // the COO copies are not needed any more
-        std::vector<uint32_t>().swap(r->rows);
-        std::vector<uint32_t>().swap(r->cols);
-        std::vector<double>().swap(r->vals);
         r->state = BUILT;
         // keep arrival order: a request becomes admissible in id order
         auto it = s->built.begin();
@@ -221,7 +241,7 @@ void dispatcher_main(acdalm_server_t * s)
                                 hv.lam_hi = m->lambda_upper.data();
                                 e = acd::alm_launch_async(a->dev, hv, s->niter, r->x.data(),
                                                           r->lam.data(), m->settings, &a->lay,
-                                                          r->launch);
+                                                          r->launch, r->team);
                         }
                         std::lock_guard<std::mutex> g(s->mu);
                         if (e) {
@@ -264,6 +284,7 @@ acdalm_server_t * acdalm_server_create(size_t device_budget, int max_inflight, i
                 device_budget = free_b / 10 * 8;
         }
         s->budget = device_budget;
+        s->max_team = acd::max_cluster_team();
         s->max_inflight = max_inflight > 0 ? max_inflight : 128;
         s->precision = precision;
         s->kkt_tol = kkt_tol;

@@ -743,7 +743,8 @@ static int alm_prepare(DevInstance & d, const HostVectors & hv, size_t niter, do
         k.a.mixed = mixed ? 1 : 0;
         k.a.min_delta32 = env_or("ACDALM_MIN_DELTA32", 1e-6);
         k.a.niter32 = (long long)env_or("ACDALM_NITER32", 200000);
-        k.a.stall_switch = (int)env_or("ACDALM_STALL_SWITCH", 3);
+        k.a.stall_switch = (int)env_or("ACDALM_STALL_SWITCH", 2);
+        k.a.pg_floor32 = env_or("ACDALM_PG_FLOOR32", 1e-6);
         if (mixed) {
                 k.M.Af = {d.m, d.a_nslices, d.a_ptr, d.a_row0, d.a_col, d.a_valf};
                 k.M.Atf = {d.n, d.at_nslices, d.at_ptr, d.at_row0, d.at_col, d.at_valf};
@@ -854,11 +855,11 @@ int run_alm(DevInstance & d, const HostVectors & hv, size_t niter, double * x,
 
 namespace {
 
-constexpr int kBatchThreads = 256;
+constexpr int kBatchThreads = 512;  // one LP per SM: 16 warps of memory parallelism
 
 // One LP on one CTA, its arguments passed by value (the server's launches).
 template <bool Exact>
-__global__ void __launch_bounds__(kBatchThreads, 2) alm_single_kernel(AlmKernelArgs k)
+__global__ void __launch_bounds__(kBatchThreads, 1) alm_single_kernel(AlmKernelArgs k)
 {
         BlockTeam tm{reinterpret_cast<int *>(&k.ctl->status_w.v)};
         Alm<BlockTeam, Exact> alm(tm, k.P, k.W, k.log, k.M);
@@ -875,7 +876,7 @@ __global__ void __launch_bounds__(kBatchThreads, 2) alm_single_kernel(AlmKernelA
 // Persistent CTAs take LPs from a shared counter (largest first) and run
 // each one's whole ALM solve with a one-CTA team.
 template <bool Exact>
-__global__ void __launch_bounds__(kBatchThreads, 2)
+__global__ void __launch_bounds__(kBatchThreads, 1)
 alm_batch_kernel(const AlmKernelArgs * items, int count, int * next)
 {
         __shared__ int cur;
@@ -904,6 +905,54 @@ alm_batch_kernel(const AlmKernelArgs * items, int count, int * next)
 
 }  // namespace
 
+// One LP on one thread-block cluster (launched with a cluster dimension).
+template <bool Exact>
+__global__ void __launch_bounds__(kBatchThreads, 1) alm_cluster_kernel(AlmKernelArgs k)
+{
+        ClusterTeam tm(reinterpret_cast<int *>(&k.ctl->status_w.v));
+        Alm<ClusterTeam, Exact> alm(tm, k.P, k.W, k.log, k.M);
+        AlmOut out;
+        memset(&out, 0, sizeof(out));
+        int r = alm.solve(k.a, k.x, k.lam, out);
+        if (tm.rank == 0 && threadIdx.x == 0) {
+                if (r < 0)
+                        out.ret = r;
+                *k.out = out;
+        }
+        // no CTA leaves while the others may still read its shared memory
+        tm.sync();
+}
+
+int max_cluster_team()
+{
+        static int cached = 0;
+        if (cached)
+                return cached;
+        const void * fn = (const void *)alm_cluster_kernel<false>;
+        cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        for (int q = 16; q >= 2; q /= 2) {
+                cudaLaunchConfig_t cfg = {};
+                cfg.gridDim = dim3(q);
+                cfg.blockDim = dim3(kBatchThreads);
+                cudaLaunchAttribute attr[1];
+                attr[0].id = cudaLaunchAttributeClusterDimension;
+                attr[0].val.clusterDim.x = q;
+                attr[0].val.clusterDim.y = 1;
+                attr[0].val.clusterDim.z = 1;
+                cfg.attrs = attr;
+                cfg.numAttrs = 1;
+                int clusters = 0;
+                if (cudaOccupancyMaxActiveClusters(&clusters, fn, &cfg) == cudaSuccess
+                    && clusters > 0) {
+                        cached = q;
+                        return q;
+                }
+                cudaGetLastError();
+        }
+        cached = 1;
+        return 1;
+}
+
 struct AlmLaunch::Impl {
         AlmKernelArgs k;
 };
@@ -918,18 +967,45 @@ AlmLaunch::~AlmLaunch()
 
 int alm_launch_async(DevInstance & d, const HostVectors & hv, size_t niter, double * x,
                      double * lam, const AlmSettings & s, const DeviceLayout * lay,
-                     AlmLaunch & h)
+                     AlmLaunch & h, int team)
 {
+        if (team < 1 || team > 16) {
+                set_error(ACDALM_EINVAL, "team of %d CTAs (1..16)", team);
+                return ACDALM_EINVAL;
+        }
         int r = alm_prepare(d, hv, niter, x, lam, false, s, lay, h.impl->k);
         if (r)
                 return r;
         if (!h.done)
                 ACD_CUDA_TRY(cudaEventCreateWithFlags(&h.done, cudaEventDisableTiming),
                              ACDALM_ECUDA);
-        if (g_exact)
-                alm_single_kernel<true><<<1, kBatchThreads, 0, d.stream>>>(h.impl->k);
-        else
-                alm_single_kernel<false><<<1, kBatchThreads, 0, d.stream>>>(h.impl->k);
+        if (team == 1) {
+                if (g_exact)
+                        alm_single_kernel<true><<<1, kBatchThreads, 0, d.stream>>>(h.impl->k);
+                else
+                        alm_single_kernel<false><<<1, kBatchThreads, 0, d.stream>>>(h.impl->k);
+        } else {
+                const void * fn = g_exact ? (const void *)alm_cluster_kernel<true>
+                                          : (const void *)alm_cluster_kernel<false>;
+                if (team > 8)
+                        ACD_CUDA_TRY(cudaFuncSetAttribute(fn,
+                                                          cudaFuncAttributeNonPortableClusterSizeAllowed,
+                                                          1), ACDALM_ECUDA);
+                cudaLaunchConfig_t cfg = {};
+                cfg.gridDim = dim3(team);
+                cfg.blockDim = dim3(kBatchThreads);
+                cfg.dynamicSmemBytes = 0;
+                cfg.stream = d.stream;
+                cudaLaunchAttribute attr[1];
+                attr[0].id = cudaLaunchAttributeClusterDimension;
+                attr[0].val.clusterDim.x = team;
+                attr[0].val.clusterDim.y = 1;
+                attr[0].val.clusterDim.z = 1;
+                cfg.attrs = attr;
+                cfg.numAttrs = 1;
+                void * params[1] = {&h.impl->k};
+                ACD_CUDA_TRY(cudaLaunchKernelExC(&cfg, fn, params), ACDALM_ECUDA);
+        }
         count_launch();
         ACD_CUDA_TRY(cudaGetLastError(), ACDALM_ECUDA);
         ACD_CUDA_TRY(cudaEventRecord(h.done, d.stream), ACDALM_ECUDA);
@@ -1216,6 +1292,32 @@ int run_mpg(DevInstance & d, const HostVectors & hv, double * x, size_t niter,
 {
         return run_inner(d, hv, x, niter, max_pg, max_value, 0, log, period, diag5,
                          offset, st, true);
+}
+
+}  // namespace acd
+
+namespace acd {
+
+// Loads every solver kernel now.  With lazy module loading the first launch
+// of a kernel can wait for all kernels already running on the device, which
+// would stall a server behind its longest solve.
+void preload_solver_kernels()
+{
+        cudaFuncAttributes a;
+        cudaFuncGetAttributes(&a, gather_kernel);
+        cudaFuncGetAttributes(&a, scatter_kernel);
+        cudaFuncGetAttributes(&a, step_size_kernel);
+        cudaFuncGetAttributes(&a, alm_kernel<false>);
+        cudaFuncGetAttributes(&a, alm_kernel<true>);
+        cudaFuncGetAttributes(&a, approx_kernel<false>);
+        cudaFuncGetAttributes(&a, approx_kernel<true>);
+        cudaFuncGetAttributes(&a, mpg_kernel);
+        cudaFuncGetAttributes(&a, alm_batch_kernel<false>);
+        cudaFuncGetAttributes(&a, alm_batch_kernel<true>);
+        cudaFuncGetAttributes(&a, alm_single_kernel<false>);
+        cudaFuncGetAttributes(&a, alm_single_kernel<true>);
+        cudaFuncGetAttributes(&a, alm_cluster_kernel<false>);
+        cudaFuncGetAttributes(&a, alm_cluster_kernel<true>);
 }
 
 }  // namespace acd

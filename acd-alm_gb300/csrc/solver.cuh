@@ -745,6 +745,7 @@ struct AlmArgs {
         int mixed;
         double min_delta32;               // the FP32 inner solves' stall test
         long long niter32;                // cap per FP32 inner solve
+        double pg_floor32;                // FP32 projected-gradient floor / |c'|
         int stall_switch;                 // FP32 stalls in a row before the
                                           // remaining outer iterations run FP64
 };
@@ -785,11 +786,11 @@ struct Alm {
         // where v = 0 and c = 0).  Partials: lambda'b, and the relative KKT
         // terms of (x, lambda) when kkt is set.
         __device__ bool penalise(const double * lam, const double * x, bool kkt,
-                                 double (&out)[6], bool write = true,
+                                 double (&out)[7], bool write = true,
                                  const AlmMixed * mx = nullptr)
         {
-                double part[6] = {0, 0, 0, 0, 0, 0};
-                const int op[6] = {RED_SUM, RED_SUM, RED_SUM, RED_SUM, RED_SUM, RED_SUM};
+                double part[7] = {0, 0, 0, 0, 0, 0, 0};
+                const int op[7] = {RED_SUM, RED_SUM, RED_SUM, RED_SUM, RED_SUM, RED_SUM, RED_SUM};
                 int lane = threadIdx.x & 31;
                 const SellDev<double> & op_t = P.At;
                 for_each_slice(tm, op_t.nslices, [&](int s) {
@@ -830,6 +831,7 @@ struct Alm {
                                                 mx->uf[j] = (float)(P.u[j] - xj);
                                                 mx->d[j] = 0.f;
                                                 part[5] += cj * xj;
+                                                part[6] += cj * cj;
                                         }
                                 }
                                 if (kkt) {
@@ -860,7 +862,7 @@ struct Alm {
                 }
                 if (!tm.reduce(part, op))
                         return false;
-                for (int k = 0; k < 6; k++)
+                for (int k = 0; k < 7; k++)
                         out[k] = part[k];
                 return true;
         }
@@ -981,7 +983,7 @@ struct Alm {
                 int ret = 1;
                 long long k;
                 bool kkt = a.kkt_tol > 0;
-                double kk[6];
+                double kk[7];
                 InnerProblem<double> ip;
                 ip.m = P.m;
                 ip.n = P.n;
@@ -996,6 +998,8 @@ struct Alm {
                 ip.inv_v = P.inv_v;
                 const AlmMixed * mx = a.mixed ? &mixed : nullptr;
                 bool fp64_inner = false;
+                bool last_was_fp32 = false;
+                double best_rk = HUGE_VAL;
                 int stalls = 0;
                 unsigned long long inner32 = 0;
                 InnerProblem<float> ipf;
@@ -1032,6 +1036,15 @@ struct Alm {
                                         ret = 0;
                                         break;
                                 }
+                                // mixed mode: FP32 inner solves that stop
+                                // improving the KKT residual hand over to FP64
+                                // (the final outer iterations refine in FP64)
+                                if (mx && !fp64_inner && last_was_fp32) {
+                                        stalls = (rk > 0.9 * best_rk) ? stalls + 1 : 0;
+                                        if (stalls >= a.stall_switch)
+                                                fp64_inner = true;
+                                }
+                                best_rk = fmin(best_rk, rk);
                         }
                         double offset = kk[0];
                         InnerArgs ia;
@@ -1061,6 +1074,9 @@ struct Alm {
                                 InnerArgs fa = ia;
                                 fa.offset = ia.offset + kk[5];
                                 fa.min_delta = fmax(ia.min_delta, a.min_delta32);
+                                // the projected gradient FP32 can resolve:
+                                // reaching it counts as reaching max_pg
+                                fa.max_pg = fmax(ia.max_pg, a.pg_floor32 * (sqrt(kk[6]) + 1));
                                 if (a.niter32 > 0 && fa.niter > a.niter32)
                                         fa.niter = a.niter32;
                                 fa.xbar = x;
@@ -1071,14 +1087,20 @@ struct Alm {
                                 inner32 += (unsigned long long)used;
                                 if (!apply_correction(x, mx->d))
                                         return -1;
-                                stalls = (reason == 2) ? 0 : stalls + 1;
-                                if (stalls >= a.stall_switch)
-                                        fp64_inner = true;
+                                last_was_fp32 = true;
+                                if (!kkt) {
+                                        // no KKT residual to watch: FP32 solves
+                                        // that stall hand over to FP64
+                                        stalls = (reason == 2) ? 0 : stalls + 1;
+                                        if (stalls >= a.stall_switch)
+                                                fp64_inner = true;
+                                }
                         } else {
                                 Approx<double, Team, Exact> ap(tm, ip, W, log);
                                 reason = ap.solve(ia, x, diag, &used);
                                 if (reason < 0)
                                         return -1;
+                                last_was_fp32 = false;
                         }
                         inner_used += (unsigned long long)used;
                         double vo[4];

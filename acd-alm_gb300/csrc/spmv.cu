@@ -635,5 +635,22 @@ int acdalm_perm_copy(struct sparse_matrix * a, int row, uint32_t * idx, uint32_t
 
 // Internal accessors used by the approx / alm layer.
 namespace acd {
+void preload_spmv_kernels()
+{
+        cudaFuncAttributes a;
+        cudaFuncGetAttributes(&a, sell_kernel<double, true>);
+        cudaFuncGetAttributes(&a, sell_kernel<float, false>);
+        cudaFuncGetAttributes(&a, sell2_kernel<double, true>);
+        cudaFuncGetAttributes(&a, sell2_kernel<float, false>);
+        cudaFuncGetAttributes(&a, block4_kernel<double>);
+        cudaFuncGetAttributes(&a, csr_kernel<double, 4>);
+        cudaFuncGetAttributes(&a, csr_kernel<double, 8>);
+        cudaFuncGetAttributes(&a, csr_kernel<double, 16>);
+        cudaFuncGetAttributes(&a, csr_kernel<double, 32>);
+        cudaFuncGetAttributes(&a, csr_kernel<float, 4>);
+        cudaFuncGetAttributes(&a, csr_kernel<float, 8>);
+        cudaFuncGetAttributes(&a, csr_kernel<float, 16>);
+        cudaFuncGetAttributes(&a, csr_kernel<float, 32>);
+}
 HostMatrix & host_of(sparse_matrix_t * m) { return m->h; }
 }

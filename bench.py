@@ -139,8 +139,8 @@ def cpu_baseline(lp, gpu_inner_per_lp: float, iters: int, threads: int):
             "cores": threads, "kind": kind,
             "sample": (f"{iters} APPROX iterations of the same LP on {threads} threads "
                        f"({dt:.1f} s, {per_iter * 1e3:.2f} ms/iteration), extrapolated to "
-                       f"{gpu_inner_per_lp:.0f} inner iterations per LP (the GPU solve's "
-                       f"count; the outer ALM work is <1% of a solve)")}
+                       f"{gpu_inner_per_lp:.0f} inner iterations per LP (the FP64 GPU solve's "
+                       f"count for the same LP; the outer ALM work is <1% of a solve)")}
 
 
 def run_reference(args, lp, rank: int):
@@ -188,9 +188,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--workload", default="mid")
-    ap.add_argument("--precision", default="fp64")
+    ap.add_argument("--precision", default="mixed")
+    ap.add_argument("--profile-solve", type=int, default=0,
+                    help="run one ALM solve capped at this many inner iterations and exit "
+                         "(the command the ncu captures use)")
     ap.add_argument("--ref-iters", type=int, default=200)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-side", action="store_true")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -213,6 +217,18 @@ def main():
 
     lib = importlib.import_module("acd-alm_gb300.lib")
     L = lib.lib()
+    if args.profile_solve:
+        m = lib.Matrix(lp)
+        alm = lib.Alm(m, lp)
+        if args.precision == "mixed":
+            alm.set_precision(lib.PRECISION_MIXED)
+        alm.set_inner_budget(args.profile_solve)
+        alm.solve(1000)
+        st = alm.stats()
+        print(json.dumps({"profile_solve": args.profile_solve, "workload": args.workload,
+                          "precision": args.precision, "inner": st["inner_iterations"],
+                          "device_seconds": st["seconds"]}))
+        return
     L.acdalm_launch_count.restype = __import__("ctypes").c_ulonglong
     m = lib.Matrix(lp)
     alm = lib.Alm(m, lp)
@@ -244,12 +260,13 @@ def main():
     clocks = ClockSampler()
     clocks.start()
     launches0 = L.acdalm_launch_count()
-    dev_s, wall_s, inner, outer, kkts = [], [], [], [], []
+    dev_s, wall_s, inner, outer, kkts, inner32 = [], [], [], [], [], []
     for _ in range(args.steps):
         r, x, lam, st, wall = one_step()
         dev_s.append(st["seconds"])
         wall_s.append(wall)
         inner.append(st["inner_iterations"])
+        inner32.append(st["fp32_inner_iterations"])
         outer.append(st["outer_iterations"])
         kkts.append(st["rel_kkt"])
     torch.cuda.synchronize()
@@ -265,9 +282,22 @@ def main():
     e2e = n_lp / tot_wall
     k = inst.rel_kkt(lp, x, lam)
     fp32 = args.precision == "mixed"
-    bpi = bytes_per_iteration(lp, fp32)
+    fp64_side = None
+    if fp32 and not args.no_fp64_side:
+        # the plain FP64 form of the same solve, for comparison
+        alm.set_precision(lib.PRECISION_FP64)
+        r64, x64, l64, st64, wall64 = one_step()
+        fp64_side = {"value": 1.0 / st64["seconds"], "unit": "LP/s",
+                     "inner_iterations": st64["inner_iterations"],
+                     "rel_kkt": st64["rel_kkt"],
+                     "objective": inst.rel_kkt(lp, x64, l64)["objective"]}
+        alm.set_precision(lib.PRECISION_MIXED)
+    bpi = bytes_per_iteration(lp, False)
+    bpi32 = bytes_per_iteration(lp, True)
     mean_inner = float(np.mean(inner))
-    algo_bytes = mean_inner * bpi
+    mean_inner32 = float(np.mean(inner32))
+    # FP32 iterations move 16 B per nonzero, FP64 ones 24 B
+    algo_bytes = mean_inner32 * bpi32 + (mean_inner - mean_inner32) * bpi
     achieved = algo_bytes / (tot_dev / args.steps) / 1e9
     peak, peak_kind = load_peaks()
     line = {
@@ -284,16 +314,20 @@ def main():
                      "unit": "GB/s", "frac": achieved / peak, "traffic": None,
                      "kernel": "alm_kernel (persistent cooperative solve)",
                      "peak_source": peak_kind,
-                     "bytes_per_inner_iteration": bpi},
+                     "bytes_per_inner_iteration": {"fp64": bpi, "fp32": bpi32}},
         "gpu_launches": int(launches),
-        "solve": {"inner_iterations": inner, "outer_iterations": outer,
+        "fp64_form": fp64_side,
+        "solve": {"inner_iterations": inner, "fp32_inner_iterations": inner32,
+                  "outer_iterations": outer,
                   "rel_kkt_device": kkts, "rel_kkt_host_check": k["rel_kkt"],
                   "objective": k["objective"], "device_seconds": dev_s,
                   "wall_seconds": wall_s},
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(lp, mean_inner, args.ref_iters,
+        # the CPU loop runs in FP64: extrapolate with the FP64 solve's count
+        per_lp = fp64_side["inner_iterations"] if fp64_side else mean_inner
+        line["cpu_baseline"] = cpu_baseline(lp, per_lp, args.ref_iters,
                                             os.cpu_count() or 1)
     if rank == 0:
         print(json.dumps(line), flush=True)

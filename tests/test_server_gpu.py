@@ -63,3 +63,17 @@ def test_budget_admits_one_at_a_time(instances):
     lps = _lps(instances, 4, 9)
     res = _serve(b, lps, device_budget=24 << 20, max_inflight=8)
     assert all(r[0] == 0 for r in res)
+
+
+def test_large_lp_runs_on_a_cluster(instances):
+    """An LP with more than 150k nonzeros is solved by a thread-block cluster
+    of CTAs; it reaches the KKT target and repeats bit for bit."""
+    b = binding()
+    lp = instances.batch_instance(12600, 77)  # 151,200 nonzeros: 4 CTAs
+    assert lp.nnz > 150000
+    first = _serve(b, [lp], max_inflight=4, precision=0)[0]
+    again = _serve(b, [lp, _lps(instances, 1, 99)[0]], max_inflight=4, precision=0)[0]
+    assert first[0] == 0
+    k = instances.rel_kkt(lp, first[1], first[2])
+    assert k["rel_kkt"] <= 1.01e-6, k
+    assert first[1].tobytes() == again[1].tobytes()

@@ -396,8 +396,9 @@ struct ClusterTeam {
 
 // A SELL operator on the device (layout.h: Sell).  Slice s starts at
 // element ptr[s] & ~31 and holds 32 >> c rows from row0[s], each spread over
-// L = 1 << c lanes, c = ptr[s] & 31; element k of its r-th row is at step
-// k >> c, lane (r << c) + (k & (L - 1)).
+// L = 1 << c lanes, c = ptr[s] & 7; per step a lane reads V consecutive
+// entries of its row: V = 4 (one int4 of columns, one float4 or two double2
+// of values) when bit 3 of ptr[s] is set, else V = 1.
 template <class V>
 struct SellDev {
         int nrows;
@@ -411,8 +412,9 @@ struct SellDev {
 // One warp's view of one slice.
 struct Slice {
         int64_t base;   // first element
-        int steps;      // 32-element steps
+        int steps;      // steps (32 V elements each)
         int shift;      // log2(lanes per row)
+        bool vec;       // V = 4
         int row;        // this lane's row (may be >= nrows: padding)
         bool lead;      // this lane owns its row's result
 };
@@ -422,12 +424,68 @@ __device__ __forceinline__ Slice slice_of(const SellDev<V> & op, int s, int lane
 {
         Slice sl;
         int64_t p0 = __ldg(op.ptr + s), p1 = __ldg(op.ptr + s + 1);
-        sl.shift = (int)(p0 & 31);
+        sl.shift = (int)(p0 & 7);
+        sl.vec = (p0 & 8) != 0;
         sl.base = p0 & ~int64_t(31);
-        sl.steps = (int)(((p1 & ~int64_t(31)) - sl.base) >> 5);
+        sl.steps = (int)(((p1 & ~int64_t(31)) - sl.base) >> (sl.vec ? 7 : 5));
         sl.row = __ldg(op.row0 + s) + (lane >> sl.shift);
         sl.lead = (lane & ((1 << sl.shift) - 1)) == 0;
         return sl;
+}
+
+// Entries per lane per step, as a type (for generic lambdas).
+template <int N>
+struct VecW {
+        static constexpr int value = N;
+};
+
+// Runs f(VecW<4>) on a vector slice, f(VecW<1>) on a scalar one.
+template <class F>
+__device__ __forceinline__ auto by_width(const Slice & sl, F && f) -> decltype(f(VecW<1>()))
+{
+        if (sl.vec)
+                return f(VecW<4>());
+        return f(VecW<1>());
+}
+
+// One lane's VEC entries of one step: columns and values.
+template <int VEC, class V>
+struct Chunk {
+        int c[VEC];
+        V a[VEC];
+};
+
+template <int VEC, class V>
+__device__ __forceinline__ Chunk<VEC, V> load_chunk(const int32_t * col, const V * val,
+                                                    int64_t at)
+{
+        Chunk<VEC, V> q;
+        if constexpr (VEC == 1) {
+                q.c[0] = __ldg(col + at);
+                q.a[0] = __ldg(val + at);
+        } else {
+                static_assert(VEC == 4, "vector slices hold 4 entries per lane");
+                int4 c = __ldg(reinterpret_cast<const int4 *>(col + at));
+                q.c[0] = c.x;
+                q.c[1] = c.y;
+                q.c[2] = c.z;
+                q.c[3] = c.w;
+                if constexpr (sizeof(V) == 8) {
+                        double2 a = __ldg(reinterpret_cast<const double2 *>(val + at));
+                        double2 b = __ldg(reinterpret_cast<const double2 *>(val + at + 2));
+                        q.a[0] = a.x;
+                        q.a[1] = a.y;
+                        q.a[2] = b.x;
+                        q.a[3] = b.y;
+                } else {
+                        float4 a = __ldg(reinterpret_cast<const float4 *>(val + at));
+                        q.a[0] = a.x;
+                        q.a[1] = a.y;
+                        q.a[2] = a.z;
+                        q.a[3] = a.w;
+                }
+        }
+        return q;
 }
 
 // Visits slices so each warp of the team gets a balanced share: slices come
@@ -455,20 +513,29 @@ __device__ __forceinline__ T lanes_tree(T v, int shift)
         return v;
 }
 
-// acc (valid in each group's first lane) += the group's L products in lane
-// order, each addition rounded: the sequential order of the row.
-__device__ __forceinline__ double lanes_in_order(double acc, double prod, int shift, int lane)
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double mul_exact(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mul_exact(float a, float b) { return __fmul_rn(a, b); }
+
+// acc (valid in each group's first lane) += the group's V L terms of one
+// step, in row order (lane by lane, V each), every addition rounded: the
+// sequential order of the row.
+template <int VEC, class T>
+__device__ __forceinline__ T in_order(T acc, const T (&p)[VEC], int shift, int lane)
 {
+        if (shift == 0) {
+#pragma unroll
+                for (int j = 0; j < VEC; j++)
+                        acc = add_rn(acc, p[j]);
+                return acc;
+        }
         int L = 1 << shift, first = lane & ~(L - 1);
-        for (int q = 0; q < L; q++)
-                acc = __dadd_rn(acc, __shfl_sync(0xffffffffu, prod, first + q));
-        return acc;
-}
-__device__ __forceinline__ float lanes_in_order(float acc, float prod, int shift, int lane)
-{
-        int L = 1 << shift, first = lane & ~(L - 1);
-        for (int q = 0; q < L; q++)
-                acc = __fadd_rn(acc, __shfl_sync(0xffffffffu, prod, first + q));
+        for (int q = 0; q < L; q++) {
+#pragma unroll
+                for (int j = 0; j < VEC; j++)
+                        acc = add_rn(acc, __shfl_sync(0xffffffffu, p[j], first + q));
+        }
         return acc;
 }
 
@@ -490,23 +557,67 @@ __device__ __forceinline__ float madd(float a, float b, float c)
         return fmaf(a, b, c);
 }
 
-__device__ __forceinline__ double mul_exact(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ float mul_exact(float a, float b) { return __fmul_rn(a, b); }
-
 // Rows longer than this, in FP32, combine their lanes' partial sums in FP64
 // (a compensated sum of the row).
 constexpr int kCompensateWidth = 256;
 
-// Finishes a row sum held as per-lane partials: tree (fast) or nothing (the
-// exact path accumulated in order already).
-template <bool Exact, class T>
-__device__ __forceinline__ T finish_row(T acc, int shift, int steps)
+// Finishes a row sum held as per-lane partials with a fixed tree; `width`
+// is the row capacity of the slice.
+template <class T>
+__device__ __forceinline__ T finish_row(T acc, int shift, int width)
 {
-        if (Exact || shift == 0)
+        if (shift == 0)
                 return acc;
-        if (sizeof(T) == 4 && (steps << shift) > kCompensateWidth)
+        if (sizeof(T) == 4 && width > kCompensateWidth)
                 return (T)lanes_tree((double)acc, shift);
         return lanes_tree(acc, shift);
+}
+
+// One row sum of a SELL slice: sum_k A_k x[col_k] for the row of this lane
+// (valid in the row's lead lane).  Exact: the row's sequential order with
+// rounded products and sums; otherwise FMA chains per lane and a tree.
+template <bool Exact, int VEC, class Team, class V, class T>
+__device__ __forceinline__ T slice_row_sum(const Team & tm, const SellDev<V> & op,
+                                           const Slice & sl, const T * x, int lane)
+{
+        int64_t at = sl.base + VEC * lane;
+        T acc = 0;
+        if constexpr (Exact) {
+                for (int t = 0; t < sl.steps; t++, at += 32 * VEC) {
+                        Chunk<VEC, V> q = load_chunk<VEC>(op.col, op.val, at);
+                        T p[VEC];
+#pragma unroll
+                        for (int j = 0; j < VEC; j++)
+                                p[j] = mul_exact((T)q.a[j], tm.ld(x + q.c[j]));
+                        acc = in_order<VEC>(acc, p, sl.shift, lane);
+                }
+                return acc;
+        } else {
+                T acc2 = 0;
+                int t = 0;
+                for (; t + 2 <= sl.steps; t += 2, at += 64 * VEC) {
+                        Chunk<VEC, V> q0 = load_chunk<VEC>(op.col, op.val, at);
+                        Chunk<VEC, V> q1 = load_chunk<VEC>(op.col, op.val, at + 32 * VEC);
+                        T x0[VEC], x1[VEC];
+#pragma unroll
+                        for (int j = 0; j < VEC; j++) {
+                                x0[j] = tm.ld(x + q0.c[j]);
+                                x1[j] = tm.ld(x + q1.c[j]);
+                        }
+#pragma unroll
+                        for (int j = 0; j < VEC; j++) {
+                                acc = madd<false>((T)q0.a[j], x0[j], acc);
+                                acc2 = madd<false>((T)q1.a[j], x1[j], acc2);
+                        }
+                }
+                if (t < sl.steps) {
+                        Chunk<VEC, V> q0 = load_chunk<VEC>(op.col, op.val, at);
+#pragma unroll
+                        for (int j = 0; j < VEC; j++)
+                                acc = madd<false>((T)q0.a[j], tm.ld(x + q0.c[j]), acc);
+                }
+                return finish_row(acc + acc2, sl.shift, (sl.steps * VEC) << sl.shift);
+        }
 }
 
 // Row sums of one SELL operator applied to x; calls epi(row, sum) in the
@@ -518,34 +629,9 @@ __device__ __forceinline__ void sell_rows_1(const Team & tm, const SellDev<V> & 
         int lane = threadIdx.x & 31;
         for_each_slice(tm, op.nslices, [&](int s) {
                 Slice sl = slice_of(op, s, lane);
-                const int32_t * cp = op.col + sl.base + lane;
-                const V * vp = op.val + sl.base + lane;
-                T acc = 0;
-                if (Exact && sl.shift) {
-                        for (int k = 0; k < sl.steps; k++) {
-                                T prod = mul_exact((T)__ldg(vp + 32 * k),
-                                                   tm.ld(x + __ldg(cp + 32 * k)));
-                                acc = lanes_in_order(acc, prod, sl.shift, lane);
-                        }
-                } else {
-                        int k = 0;
-                        for (; k + 4 <= sl.steps; k += 4) {
-                                int c0 = __ldg(cp + 32 * k), c1 = __ldg(cp + 32 * (k + 1)),
-                                    c2 = __ldg(cp + 32 * (k + 2)), c3 = __ldg(cp + 32 * (k + 3));
-                                T v0 = (T)__ldg(vp + 32 * k), v1 = (T)__ldg(vp + 32 * (k + 1)),
-                                  v2 = (T)__ldg(vp + 32 * (k + 2)), v3 = (T)__ldg(vp + 32 * (k + 3));
-                                T x0 = tm.ld(x + c0), x1 = tm.ld(x + c1),
-                                  x2 = tm.ld(x + c2), x3 = tm.ld(x + c3);
-                                acc = madd<Exact>(v0, x0, acc);
-                                acc = madd<Exact>(v1, x1, acc);
-                                acc = madd<Exact>(v2, x2, acc);
-                                acc = madd<Exact>(v3, x3, acc);
-                        }
-                        for (; k < sl.steps; k++)
-                                acc = madd<Exact>((T)__ldg(vp + 32 * k),
-                                                  tm.ld(x + __ldg(cp + 32 * k)), acc);
-                        acc = finish_row<Exact>(acc, sl.shift, sl.steps);
-                }
+                T acc = by_width(sl, [&](auto w) {
+                        return slice_row_sum<Exact, decltype(w)::value>(tm, op, sl, x, lane);
+                });
                 if (sl.lead && sl.row < op.nrows)
                         epi(sl.row, acc);
         });
@@ -559,37 +645,41 @@ __device__ __forceinline__ void sell_rows_2(const Team & tm, const SellDev<V> & 
         int lane = threadIdx.x & 31;
         for_each_slice(tm, op.nslices, [&](int s) {
                 Slice sl = slice_of(op, s, lane);
-                const int32_t * cp = op.col + sl.base + lane;
-                const V * vp = op.val + sl.base + lane;
                 T a0 = 0, a1 = 0;
-                if (Exact && sl.shift) {
-                        for (int k = 0; k < sl.steps; k++) {
-                                int c = __ldg(cp + 32 * k);
-                                T v = (T)__ldg(vp + 32 * k);
-                                a0 = lanes_in_order(a0, mul_exact(v, tm.ld(x0 + c)), sl.shift, lane);
-                                a1 = lanes_in_order(a1, mul_exact(v, tm.ld(x1 + c)), sl.shift, lane);
+                by_width(sl, [&](auto w) {
+                        constexpr int VEC = decltype(w)::value;
+                        int64_t at = sl.base + VEC * lane;
+                        for (int t = 0; t < sl.steps; t++, at += 32 * VEC) {
+                                Chunk<VEC, V> q = load_chunk<VEC>(op.col, op.val, at);
+                                T p[VEC], r[VEC];
+#pragma unroll
+                                for (int j = 0; j < VEC; j++) {
+                                        p[j] = tm.ld(x0 + q.c[j]);
+                                        r[j] = tm.ld(x1 + q.c[j]);
+                                }
+                                if constexpr (Exact) {
+#pragma unroll
+                                        for (int j = 0; j < VEC; j++) {
+                                                p[j] = mul_exact((T)q.a[j], p[j]);
+                                                r[j] = mul_exact((T)q.a[j], r[j]);
+                                        }
+                                        a0 = in_order<VEC>(a0, p, sl.shift, lane);
+                                        a1 = in_order<VEC>(a1, r, sl.shift, lane);
+                                } else {
+#pragma unroll
+                                        for (int j = 0; j < VEC; j++) {
+                                                a0 = madd<false>((T)q.a[j], p[j], a0);
+                                                a1 = madd<false>((T)q.a[j], r[j], a1);
+                                        }
+                                }
                         }
-                } else {
-                        int k = 0;
-                        for (; k + 2 <= sl.steps; k += 2) {
-                                int c0 = __ldg(cp + 32 * k), c1 = __ldg(cp + 32 * (k + 1));
-                                T v0 = (T)__ldg(vp + 32 * k), v1 = (T)__ldg(vp + 32 * (k + 1));
-                                T p0 = tm.ld(x0 + c0), q0 = tm.ld(x1 + c0);
-                                T p1 = tm.ld(x0 + c1), q1 = tm.ld(x1 + c1);
-                                a0 = madd<Exact>(v0, p0, a0);
-                                a1 = madd<Exact>(v0, q0, a1);
-                                a0 = madd<Exact>(v1, p1, a0);
-                                a1 = madd<Exact>(v1, q1, a1);
+                        if constexpr (!Exact) {
+                                int width = (sl.steps * VEC) << sl.shift;
+                                a0 = finish_row(a0, sl.shift, width);
+                                a1 = finish_row(a1, sl.shift, width);
                         }
-                        for (; k < sl.steps; k++) {
-                                int c = __ldg(cp + 32 * k);
-                                T v = (T)__ldg(vp + 32 * k);
-                                a0 = madd<Exact>(v, tm.ld(x0 + c), a0);
-                                a1 = madd<Exact>(v, tm.ld(x1 + c), a1);
-                        }
-                        a0 = finish_row<Exact>(a0, sl.shift, sl.steps);
-                        a1 = finish_row<Exact>(a1, sl.shift, sl.steps);
-                }
+                        return 0;
+                });
                 if (sl.lead && sl.row < op.nrows)
                         epi(sl.row, a0, a1);
         });

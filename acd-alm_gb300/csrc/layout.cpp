@@ -2,6 +2,7 @@
 #include "layout.h"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 
@@ -14,6 +15,8 @@ constexpr size_t kBlockRing = 16;      // spmv_block.c:143-145
 constexpr size_t kBlockHeader = 32;    // sizeof(struct matrix_subblock)
 constexpr size_t kSortWindow = 256;    // permutation.c:59-61
 constexpr int kSlice = 32;             // rows per SELL slice (one warp)
+constexpr int kVec = 4;                // entries per lane per step, vector slices
+constexpr int64_t kVecFlag = 8;        // slice pointer bit: vector slice
 
 // permutation.c:63-125: nonzeros per index; each window of 256 sorted by
 // (count, original index).  A stable counting of the window by count gives
@@ -288,6 +291,22 @@ int log2i(int v)
         return r;
 }
 
+// How slices pick between scalar lanes (one entry per lane per step) and
+// vector lanes (4 consecutive entries per lane per step, 16-byte loads):
+// ACDALM_SELL_VEC=0 never vectorises, 1 always, unset / "auto" vectorises a
+// slice when its rows' capacity grows by at most 1/8 over the scalar
+// form's (rounding a row up to a multiple of 4L adds padding, and every
+// padding entry still costs a gather).
+int vector_mode()
+{
+        const char * e = getenv("ACDALM_SELL_VEC");
+        if (e && e[0] == '0')
+                return 0;
+        if (e && e[0] == '1')
+                return 1;
+        return 2;
+}
+
 // One SELL operator: device row d is CSR row src_of_d[d] (rows already in
 // decreasing length); its entries keep their CSR order, columns mapped
 // through col_map (identity if empty).
@@ -295,26 +314,34 @@ void build_sell(Sell & s, const Csr & c, const std::vector<int32_t> & src_of_d,
                 const std::vector<int32_t> & col_map)
 {
         int n = (int)src_of_d.size();
+        int mode = vector_mode();
         s.nrows = n;
         s.ptr.clear();
         s.row0.clear();
         s.max_width = 0;
         auto len_of = [&](int d) { return c.ptr[src_of_d[d] + 1] - c.ptr[src_of_d[d]]; };
-        std::vector<int> lanes;
+        auto cdiv = [](uint32_t a, uint32_t b) { return (a + b - 1) / b; };
+        struct Shape {
+                int L, vec;
+        };
+        std::vector<Shape> shape;
         int64_t off = 0;
         for (int d = 0; d < n;) {
                 uint32_t first = len_of(d);
-                int L = lanes_for(first);
+                int L1 = lanes_for(first), L4 = lanes_for(cdiv(first, kVec));
+                uint32_t cap1 = cdiv(first, L1) * L1, cap4 = cdiv(first, kVec * L4) * kVec * L4;
+                bool vec = mode == 1 || (mode == 2 && 8 * (uint64_t)cap4 <= 9 * (uint64_t)cap1);
+                int L = vec ? L4 : L1, V = vec ? kVec : 1;
                 int h = kSlice / L;
                 uint32_t w = 0;
                 for (int r = d; r < std::min(n, d + h); r++)
                         w = std::max(w, len_of(r));
                 s.max_width = std::max(s.max_width, (int)w);
-                int steps = (int)((w + L - 1) / L);
-                s.ptr.push_back(off | log2i(L));
+                int64_t steps = cdiv(w, (uint32_t)(V * L));
+                s.ptr.push_back(off | log2i(L) | (vec ? kVecFlag : 0));
                 s.row0.push_back(d);
-                lanes.push_back(L);
-                off += (int64_t)steps * kSlice;
+                shape.push_back({L, V});
+                off += steps * kSlice * V;
                 d += h;
         }
         s.nslices = (int)s.row0.size();
@@ -324,10 +351,19 @@ void build_sell(Sell & s, const Csr & c, const std::vector<int32_t> & src_of_d,
         auto map = [&](uint32_t cc) {
                 return col_map.empty() ? (int32_t)cc : col_map[cc];
         };
+        // entry k of row r of a slice: step k / (V L), lane r L + (k / V) % L,
+        // sub-slot k % V
+        auto at = [](int64_t base, Shape sh, int r, uint32_t k) {
+                int64_t step = k / (sh.vec * sh.L);
+                int q = r * sh.L + (int)((k / sh.vec) % sh.L);
+                return base + step * (kSlice * sh.vec) + q * sh.vec + k % sh.vec;
+        };
         for (int sl = 0; sl < s.nslices; sl++) {
-                int64_t base = s.ptr[sl] & ~int64_t(31);
-                int L = lanes[sl], h = kSlice / L;
-                int steps = (int)(((s.ptr[sl + 1] & ~int64_t(31)) - base) / kSlice);
+                int64_t base = s.ptr[sl] & ~int64_t(kSlice - 1);
+                Shape sh = shape[sl];
+                int h = kSlice / sh.L;
+                int64_t end = s.ptr[sl + 1] & ~int64_t(kSlice - 1);
+                uint32_t slots = (uint32_t)((end - base) / kSlice) * sh.L;
                 int d0 = s.row0[sl];
                 int32_t slice_pad = 0;
                 for (int r = 0; r < h && d0 + r < n; r++) {
@@ -344,16 +380,16 @@ void build_sell(Sell & s, const Csr & c, const std::vector<int32_t> & src_of_d,
                         if (d < n) {
                                 int src = src_of_d[d];
                                 for (uint32_t j = c.ptr[src]; j < c.ptr[src + 1]; j++, k++) {
-                                        int64_t at = base + (int64_t)(k / L) * kSlice + r * L + k % L;
-                                        s.col[at] = map(c.col[j]);
-                                        s.val[at] = c.val[j];
-                                        pad = s.col[at];
+                                        int64_t o = at(base, sh, r, k);
+                                        s.col[o] = map(c.col[j]);
+                                        s.val[o] = c.val[j];
+                                        pad = s.col[o];
                                 }
                         }
                         // padding: value 0, a column of this row (or slice),
                         // so the gather stays in cache and in bounds
-                        for (; k < (uint32_t)steps * L; k++)
-                                s.col[base + (int64_t)(k / L) * kSlice + r * L + k % L] = pad;
+                        for (; k < slots; k++)
+                                s.col[at(base, sh, r, k)] = pad;
                 }
         }
 }

@@ -57,18 +57,23 @@ void ensure_blocks(HostMatrix & m);
 void ensure_zorder(HostMatrix & m);
 
 // Warp-sliced ELL of one operator (A or A') in device order, with a
-// per-slice height.  A slice is 32 lanes wide; it holds h = 32 / L
-// consecutive rows, each row spread over L lanes (L = 1, 4, 16 or 32, chosen
-// from the slice's longest row so no slice needs more than ~16 steps).
-// Element k of the slice's r-th row sits at step k / L, lane r * L + k % L,
-// i.e. at offset ptr + 32 * (k / L) + r * L + k % L.  ptr is a multiple of
-// 32; its low 5 bits hold log2(L).
+// per-slice height and lane width.  A slice is 32 lanes wide and holds
+// h = 32 / L consecutive rows, each row spread over L lanes (L = 1, 4, 16 or
+// 32, chosen from the slice's longest row).  A slice is either scalar (a
+// lane holds V = 1 entry of its row per step) or vector (V = 4 consecutive
+// entries per step, so one 16-byte load fetches 4 column indices and one or
+// two 16-byte loads their values).  Entry k of the slice's r-th row sits at
+// step t = k / (V L), lane q = r L + (k / V) % L, sub-slot k % V, i.e. at
+// offset base + 32 V t + V q + k % V.  base = ptr & ~31; the low bits of ptr
+// hold log2(L) (bits 0-2) and V = 4 (bit 3).  Within a row, entries keep
+// their order (a lane's V entries are consecutive, lanes follow each
+// other); padding entries have value 0 and a column of the row.
 struct Sell {
         int nrows = 0;                 // rows of the operator
         int nslices = 0;
         std::vector<int64_t> ptr;      // nslices + 1: element offset | log2(L)
         std::vector<int32_t> row0;     // nslices: first row of each slice
-        std::vector<int32_t> col;      // ptr[nslices] >> 5 << 5
+        std::vector<int32_t> col;      // ptr[nslices] entries
         std::vector<double> val;
         int max_width = 0;
 };

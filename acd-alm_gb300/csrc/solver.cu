@@ -52,13 +52,22 @@ __global__ void step_size_kernel(SellDev<double> at, const double * w,
         int nwarps = (gridDim.x * blockDim.x) >> 5;
         for (int s = warp; s < at.nslices; s += nwarps) {
                 Slice sl = slice_of(at, s, lane);
-                double acc = 0;
-                for (int k = 0; k < sl.steps; k++) {
-                        int i = at.col[sl.base + 32 * k + lane];
-                        double a = at.val[sl.base + 32 * k + lane];
-                        double t = __dmul_rn(__dmul_rn(__dmul_rn(w[i], beta[i]), a), a);
-                        acc = lanes_in_order(acc, t, sl.shift, lane);
-                }
+                double acc = by_width(sl, [&](auto wv) {
+                        constexpr int VEC = decltype(wv)::value;
+                        int64_t e = sl.base + VEC * lane;
+                        double sum = 0;
+                        for (int k = 0; k < sl.steps; k++, e += 32 * VEC) {
+                                Chunk<VEC, double> q = load_chunk<VEC>(at.col, at.val, e);
+                                double t[VEC];
+#pragma unroll
+                                for (int j = 0; j < VEC; j++)
+                                        t[j] = __dmul_rn(__dmul_rn(__dmul_rn(w[q.c[j]], beta[q.c[j]]),
+                                                                   q.a[j]),
+                                                         q.a[j]);
+                                sum = in_order<VEC>(sum, t, sl.shift, lane);
+                        }
+                        return sum;
+                });
                 int j = sl.row;
                 if (sl.lead && j < at.nrows) {
                         v[j] = acc;

@@ -795,23 +795,40 @@ struct Alm {
                 const SellDev<double> & op_t = P.At;
                 for_each_slice(tm, op_t.nslices, [&](int s) {
                         Slice sl = slice_of(op_t, s, lane);
-                        const int32_t * cp = op_t.col + sl.base + lane;
-                        const double * vp = op_t.val + sl.base + lane;
                         double acc = 0, vv = 0;
-                        for (int k = 0; k < sl.steps; k++) {
-                                int i = __ldg(cp + 32 * k);
-                                double a = __ldg(vp + 32 * k);
-                                // v in the reference's order and rounding
-                                double t = __dmul_rn(__dmul_rn(__dmul_rn(tm.ld(P.w + i),
-                                                                         P.beta[i]), a), a);
-                                vv = lanes_in_order(vv, t, sl.shift, lane);
-                                if (Exact)
-                                        acc = lanes_in_order(acc, __dmul_rn(a, tm.ld(lam + i)),
-                                                             sl.shift, lane);
-                                else
-                                        acc = fma(a, tm.ld(lam + i), acc);
-                        }
-                        acc = finish_row<Exact>(acc, sl.shift, sl.steps);
+                        by_width(sl, [&](auto wv) {
+                                constexpr int VEC = decltype(wv)::value;
+                                int64_t at = sl.base + VEC * lane;
+                                for (int k = 0; k < sl.steps; k++, at += 32 * VEC) {
+                                        Chunk<VEC, double> q =
+                                                load_chunk<VEC>(op_t.col, op_t.val, at);
+                                        double t[VEC], pl[VEC];
+#pragma unroll
+                                        for (int j = 0; j < VEC; j++) {
+                                                int i = q.c[j];
+                                                // v in the reference's order and rounding
+                                                t[j] = __dmul_rn(__dmul_rn(__dmul_rn(tm.ld(P.w + i),
+                                                                                     P.beta[i]),
+                                                                           q.a[j]),
+                                                                 q.a[j]);
+                                                pl[j] = tm.ld(lam + i);
+                                        }
+                                        vv = in_order<VEC>(vv, t, sl.shift, lane);
+                                        if constexpr (Exact) {
+#pragma unroll
+                                                for (int j = 0; j < VEC; j++)
+                                                        pl[j] = __dmul_rn(q.a[j], pl[j]);
+                                                acc = in_order<VEC>(acc, pl, sl.shift, lane);
+                                        } else {
+#pragma unroll
+                                                for (int j = 0; j < VEC; j++)
+                                                        acc = fma(q.a[j], pl[j], acc);
+                                        }
+                                }
+                                if constexpr (!Exact)
+                                        acc = finish_row(acc, sl.shift, (sl.steps * VEC) << sl.shift);
+                                return 0;
+                        });
                         int j = sl.row;
                         if (sl.lead && j < P.n) {
                                 double cj = P.c0[j] - acc;

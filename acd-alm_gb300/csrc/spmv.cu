@@ -620,6 +620,39 @@ int acdalm_csr_copy(struct sparse_matrix * a, int transpose, uint32_t * rows_ind
         return 0;
 }
 
+int acdalm_sell_copy(struct sparse_matrix * a, int transpose, size_t * nslices,
+                     size_t * nelems, int64_t * ptr, int32_t * row0, int32_t * columns,
+                     double * values, int32_t * row_of_d)
+{
+        if (!a || !nslices || !nelems) {
+                acd::set_error(ACDALM_EINVAL, "acdalm_sell_copy: null argument");
+                return ACDALM_EINVAL;
+        }
+        acd::PlainSell ps;
+        acd::build_plain_sell(a->h, transpose != 0, ps);
+        size_t ns = (size_t)ps.s.nslices, ne = (size_t)ps.s.ptr.back();
+        if (ptr) {
+                if (*nslices < ns || *nelems < ne) {
+                        acd::set_error(ACDALM_EINVAL,
+                                       "acdalm_sell_copy: %zu slices and %zu elements needed",
+                                       ns, ne);
+                        return ACDALM_EINVAL;
+                }
+                memcpy(ptr, ps.s.ptr.data(), (ns + 1) * sizeof(int64_t));
+                if (ns)
+                        memcpy(row0, ps.s.row0.data(), ns * sizeof(int32_t));
+                if (ne) {
+                        memcpy(columns, ps.s.col.data(), ne * sizeof(int32_t));
+                        memcpy(values, ps.s.val.data(), ne * sizeof(double));
+                }
+                if (!ps.row_of_d.empty())
+                        memcpy(row_of_d, ps.row_of_d.data(), ps.row_of_d.size() * sizeof(int32_t));
+        }
+        *nslices = ns;
+        *nelems = ne;
+        return 0;
+}
+
 int acdalm_perm_copy(struct sparse_matrix * a, int row, uint32_t * idx, uint32_t * ridx)
 {
         const acd::Perm & p = row ? a->h.rperm : a->h.cperm;

@@ -104,6 +104,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.acdalm_block_copy.argtypes = [_vp, C.c_int, _u64p, _vp, _sz]
     L.acdalm_csr_copy.argtypes = [_vp, C.c_int, _u32p, _u32p, _f64p]
     L.acdalm_perm_copy.argtypes = [_vp, C.c_int, _u32p, _u32p]
+    L.acdalm_sell_copy.argtypes = [_vp, C.c_int, C.POINTER(_sz), C.POINTER(_sz), _vp, _vp,
+                                   _vp, _vp, _vp]
     L.acdalm_approx_permuted_matrix.restype = _vp
     L.acdalm_approx_permuted_matrix.argtypes = [_vp]
     L.acdalm_approx_step_sizes.argtypes = [_vp, _f64p, _f64p, _f64p]
@@ -211,6 +213,29 @@ class Matrix:
             ridx = np.zeros(n, np.uint32)
             L.acdalm_perm_copy(self.h, row, idx, ridx)
             out["rperm" if row else "cperm"] = (idx, ridx)
+        return out
+
+    def sell(self, transpose: bool) -> dict:
+        """The SELL layout of A (or A') the SELL SpMV variant uploads:
+        ptr, row0, col, val and row_of_d (device row -> matrix row)."""
+        L = lib()
+        ns, ne = _sz(), _sz()
+        check(L.acdalm_sell_copy(self.h, int(transpose), C.byref(ns), C.byref(ne),
+                                 None, None, None, None, None), "acdalm_sell_copy")
+        nrows = self.ncols if transpose else self.nrows
+        out = {"ptr": np.zeros(ns.value + 1, np.int64),
+               "row0": np.zeros(max(ns.value, 1), np.int32),
+               "col": np.zeros(max(ne.value, 1), np.int32),
+               "val": np.zeros(max(ne.value, 1)),
+               "row_of_d": np.zeros(max(nrows, 1), np.int32)}
+        check(L.acdalm_sell_copy(self.h, int(transpose), C.byref(ns), C.byref(ne),
+                                 *(out[k].ctypes.data_as(_vp)
+                                   for k in ("ptr", "row0", "col", "val", "row_of_d"))),
+              "acdalm_sell_copy")
+        out["row0"] = out["row0"][:ns.value]
+        out["col"] = out["col"][:ne.value]
+        out["val"] = out["val"][:ne.value]
+        out["row_of_d"] = out["row_of_d"][:nrows]
         return out
 
     def multiply(self, x, transpose=False):

@@ -52,7 +52,69 @@ def workload(name: str):
         return inst.mid()
     if name == "small":
         return inst.small()
+    if name == "covering":
+        return inst.covering()
     raise SystemExit(f"unknown workload {name}")
+
+
+def spmv_bench(args, lp):
+    """--spmv: y = A x and y = A'x on the device, every layout variant, FP64
+    and FP32, L2 flushed before each timed launch; GB/s from the algorithmic
+    bytes nnz*(value+4) + 4*(rows+1) + value*(rows+cols)."""
+    import torch
+    lib = importlib.import_module("acd-alm_gb300.lib")
+    L = lib.lib()
+    m = lib.Matrix(lp)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    peak, peak_kind = load_peaks()
+    names = {0: "sell", 1: "block", 2: "csr"}
+    out = []
+    for variant in (0, 2, 1):
+        for t in (0, 1):
+            for f32 in (False, True):
+                if variant == 1 and f32:
+                    continue
+                dt = torch.float32 if f32 else torch.float64
+                nx, ny = (lp.nrows, lp.ncols) if t else (lp.ncols, lp.nrows)
+                x = torch.rand(nx, dtype=dt, device="cuda")
+                y = torch.empty(ny, dtype=dt, device="cuda")
+                fn = L.acdalm_spmv_device_f32 if f32 else L.acdalm_spmv_device
+                for _ in range(3):
+                    lib.check(fn(m.h, variant, t, x.data_ptr(), y.data_ptr(), stream.cuda_stream),
+                              "spmv")
+                times = []
+                for _ in range(args.spmv_reps):
+                    flush.fill_(1.0)
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    fn(m.h, variant, t, x.data_ptr(), y.data_ptr(), stream.cuda_stream)
+                    e1.record(stream)
+                    torch.cuda.synchronize()
+                    times.append(e0.elapsed_time(e1) * 1e-3)
+                sec = statistics.median(times)
+                sv = 4 if f32 else 8
+                nbytes = lp.nnz * (sv + 4) + 4 * (ny + 1) + sv * (nx + ny)
+                out.append({"variant": names[variant], "op": "A'x" if t else "Ax",
+                            "dtype": "f32" if f32 else "f64", "us": round(sec * 1e6, 1),
+                            "gbs": round(nbytes / sec / 1e9, 1),
+                            "frac": round(nbytes / sec / 1e9 / peak, 3),
+                            "exact": (not f32) and variant in (0, 1)})
+    best = max(out, key=lambda r: r["gbs"])
+    line = {"metric": "SpMV HBM GB/s (covering LP)", "value": best["gbs"], "unit": "GB/s",
+            "n_gpus": 1, "steps": args.spmv_reps, "warmup": 3,
+            "ms_per_step": best["us"] / 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": best["dtype"], "data": "synthetic",
+            "config": {"workload": "covering LP", "m": lp.nrows, "n": lp.ncols, "nnz": lp.nnz,
+                       "l2": "flushed (512 MB write) before every launch"},
+            "roofline": {"bound": "hbm", "achieved": best["gbs"], "peak": peak, "unit": "GB/s",
+                         "frac": best["gbs"] / peak, "traffic": None,
+                         "kernel": f"{best['variant']} {best['op']} {best['dtype']}",
+                         "peak_source": peak_kind},
+            "variants": out}
+    print(json.dumps(line), flush=True)
+    m.free()
 
 
 def bytes_per_iteration(lp, fp32: bool) -> float:
@@ -195,6 +257,9 @@ def main():
     ap.add_argument("--ref-iters", type=int, default=200)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-side", action="store_true")
+    ap.add_argument("--spmv", action="store_true",
+                    help="time the device SpMV variants on the workload's matrix")
+    ap.add_argument("--spmv-reps", type=int, default=10)
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -204,6 +269,10 @@ def main():
     if args.impl == "reference":
         if rank == 0:
             run_reference(args, lp, rank)
+        return
+
+    if args.spmv:
+        spmv_bench(args, lp)
         return
 
     import torch

@@ -158,6 +158,19 @@ int acdalm_block_copy(struct sparse_matrix * a, int transpose,
 int acdalm_csr_copy(struct sparse_matrix * a, int transpose,
                     uint32_t * rows_indices, uint32_t * columns,
                     double * values);
+/* The warp-sliced ELL ("SELL") layout the ACDALM_SPMV_SELL variant uploads
+ * for A (transpose = 0) or A' (1); no reference counterpart.  Slice s holds
+ * 32 / L rows from device row row0[s], L = 1 << (ptr[s] & 127) lanes per
+ * row; entry k of the slice's r-th row is element (ptr[s] & ~127) +
+ * 128 (k / 4L) + 4 (r L + (k / 4) % L) + k % 4 of columns / values;
+ * padding entries have value 0.  Device row d is matrix row row_of_d[d].
+ * With ptr NULL, stores the slice and element counts only; otherwise
+ * *nslices and *nelems give the capacities of row0 (nslices), ptr
+ * (nslices + 1), columns and values (nelems); row_of_d holds one entry per
+ * row of the operator. */
+int acdalm_sell_copy(struct sparse_matrix * a, int transpose, size_t * nslices,
+                     size_t * nelems, int64_t * ptr, int32_t * row0,
+                     int32_t * columns, double * values, int32_t * row_of_d);
 /* Row (row = 1) or column permutation, idx = new -> old, ridx = old -> new
  * (spmv/permutation.c:63-125). */
 int acdalm_perm_copy(struct sparse_matrix * a, int row, uint32_t * idx,

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 from golden_io import GOLDEN, load_lp
-from libutil import binding
+from libutil import binding, ragged_lp
 
 
 def sha(a):
@@ -96,4 +96,62 @@ def test_permute_vectors(instances):
     assert L.sparse_matrix_col_permute(m.h, back, lp.ncols, dst, -1) == 0
     assert (back == src).all()
     assert L.sparse_matrix_col_permute(m.h, back, lp.ncols - 1, dst, -1) == 1
+    m.free()
+
+
+def _decode_sell(s, nrows):
+    """Row d of the SELL layout as (columns, values), padding included, and
+    the number of vector slices."""
+    out = {}
+    ptr = s["ptr"]
+    nvec = 0
+    for sl in range(len(s["row0"])):
+        L = 1 << int(ptr[sl] & 7)
+        V = 4 if ptr[sl] & 8 else 1
+        nvec += V == 4
+        base = int(ptr[sl]) & ~31
+        span = (int(ptr[sl + 1]) & ~31) - base
+        assert span % (32 * V) == 0
+        steps = span // (32 * V)
+        for r in range(32 // L):
+            d = int(s["row0"][sl]) + r
+            k = np.arange(steps * V * L)
+            at = base + 32 * V * (k // (V * L)) + V * (r * L + (k // V) % L) + k % V
+            out[d] = (s["col"][at], s["val"][at])
+    assert sorted(out) == list(range(len(out))) and len(out) >= nrows
+    return out, nvec
+
+
+@pytest.mark.parametrize("mode", ["0", "1", "auto"])
+@pytest.mark.parametrize("transpose", [False, True])
+def test_sell_layout_holds_every_row_in_order(instances, transpose, mode, monkeypatch):
+    """The SELL layout (scalar slices: 1 entry per lane per step; vector
+    slices: 4) holds each row's entries in CSR order followed by
+    zero-valued padding whose columns are in range; rows are in decreasing
+    length.  ACDALM_SELL_VEC picks scalar (0), vector (1) or per-slice
+    (auto) slices."""
+    b = binding()
+    lp = ragged_lp(instances, 4)
+    m = b.Matrix(lp)
+    monkeypatch.setenv("ACDALM_SELL_VEC", mode)
+    s = m.sell(transpose)
+    ri, cc, vv = m.layouts()[f"csr{int(transpose)}"]
+    nrows, ncols = (lp.ncols, lp.nrows) if transpose else (lp.nrows, lp.ncols)
+    rows, nvec = _decode_sell(s, nrows)
+    nslices = len(s["row0"])
+    assert nvec == {"0": 0, "1": nslices}.get(mode, nvec)
+    if mode == "auto":
+        assert 0 < nvec < nslices
+    assert sorted(s["row_of_d"]) == list(range(nrows))
+    lens = np.diff(ri.astype(np.int64))
+    assert (np.diff(lens[s["row_of_d"]]) <= 0).all()
+    for d in range(nrows):
+        r = s["row_of_d"][d]
+        k = lens[r]
+        c, v = rows[d]
+        assert (c[:k] == cc[ri[r]:ri[r + 1]]).all() and (v[:k] == vv[ri[r]:ri[r + 1]]).all()
+        assert (v[k:] == 0).all() and (c >= 0).all() and (c < ncols).all()
+    for d in range(nrows, len(rows)):
+        c, v = rows[d]
+        assert (v == 0).all() and (c >= 0).all() and (c < ncols).all()
     m.free()

@@ -16,7 +16,7 @@ import numpy as np
 import pytest
 
 from golden_io import GOLDEN, load_lp
-from libutil import binding
+from libutil import binding, ragged_lp
 
 pytestmark = pytest.mark.gpu
 
@@ -56,6 +56,34 @@ def test_step_sizes_bit_identical(oracle_lib, instances):
         oracle_lib.matrix_free(mo)
         a.free()
         m.free()
+
+
+@pytest.mark.parametrize("mode", ["0", "1", "auto"])
+def test_step_sizes_bit_identical_all_slice_kinds(mode, oracle_lib, instances, monkeypatch):
+    """v_j = sum_i w_i beta_i A_ij^2 stays bit-identical whether the A'
+    slices hold 1 or 4 entries per lane and step (ACDALM_SELL_VEC)."""
+    monkeypatch.setenv("ACDALM_SELL_VEC", mode)
+    b = binding()
+    lp = ragged_lp(instances, 22)
+    # transpose so that A' has the ragged rows
+    lp = instances.LP(lp.ncols, lp.nrows, lp.cols.copy(), lp.rows.copy(), lp.vals.copy(),
+                      np.zeros(lp.ncols), np.zeros(lp.nrows), np.zeros(lp.nrows),
+                      np.ones(lp.nrows), np.full(lp.ncols, -np.inf),
+                      np.full(lp.ncols, np.inf), "ragged_t", 22)
+    w = np.random.default_rng(5).uniform(0.5, 3, lp.nrows)
+    m = b.Matrix(lp)
+    a = b.Approx(m, lp, weight=w)
+    beta, v, inv_v = a.step_sizes()
+    mo = oracle_lib.matrix(lp, 0)
+    ao = oracle_lib.approx(mo, lp, weight=w)
+    internals = oracle_lib.internals(ao, lp.nrows, lp.ncols, True)
+    cridx = a.permuted_matrix().layouts()["cperm"][1]
+    assert v.tobytes() == internals["v"][cridx].tobytes()
+    assert inv_v.tobytes() == internals["inv_v"][cridx].tobytes()
+    oracle_lib.approx_free(ao)
+    oracle_lib.matrix_free(mo)
+    a.free()
+    m.free()
 
 
 @pytest.mark.parametrize("niter", [1, 2, 10, 40])

@@ -31,6 +31,70 @@ constexpr int kStatusNonFinite = -5;                 // ACDALM_ENONFINITE
 
 enum RedOp { RED_SUM = 0, RED_MAX = 1, RED_MIN = 2 };
 
+// A float-float number hi + lo (|lo| <= ulp(hi) / 2 after normalisation):
+// the FP32 inner solve accumulates its reduction partials in this form on
+// the FP32 pipe, which is many times wider than the FP64 pipe of this GPU.
+// A product of two floats is carried exactly (Dekker's two-product via one
+// fused multiply-add), sums use Knuth's two-sum, so a partial over a few
+// hundred terms keeps about 44 bits.
+struct DF {
+        float hi, lo;
+};
+
+// a + b exactly as s + e (Knuth's two-sum; no multiplications, so nothing
+// is contracted).
+__device__ __forceinline__ void two_sum(float a, float b, float & s, float & e)
+{
+        s = a + b;
+        float bb = s - a;
+        e = (a - (s - bb)) + (b - bb);
+}
+
+__device__ __forceinline__ DF df_add(DF a, DF b)
+{
+        float s, e;
+        two_sum(a.hi, b.hi, s, e);
+        e += a.lo + b.lo;
+        float h = s + e;
+        return {h, e - (h - s)};
+}
+
+// Partial accumulators: double for the FP64 solve, DF for the FP32 one.
+__device__ __forceinline__ void acc_add(double & a, double x) { a += x; }
+__device__ __forceinline__ void acc_prod(double & a, double x, double y) { a += x * y; }
+__device__ __forceinline__ void acc_max(double & a, double x) { a = (x > a) ? x : a; }
+
+__device__ __forceinline__ void acc_add(DF & a, float x)
+{
+        float s, e;
+        two_sum(a.hi, x, s, e);
+        a.hi = s;
+        a.lo += e;
+}
+
+// a += x for a double term of the FP32 solve (the rare terms that involve
+// the FP64 point): x split into two floats.
+__device__ __forceinline__ void acc_add(DF & a, double x)
+{
+        float h = (float)x;
+        acc_add(a, h);
+        a.lo += (float)(x - (double)h);
+}
+
+__device__ __forceinline__ void acc_prod(DF & a, float x, float y)
+{
+        float p = __fmul_rn(x, y);
+        float pe = fmaf(x, y, -p);  // exact: x y = p + pe
+        acc_add(a, p);
+        a.lo += pe;
+}
+
+__device__ __forceinline__ void acc_max(DF & a, float x)
+{
+        if (x > a.hi)
+                a = {x, 0.f};
+}
+
 __device__ __forceinline__ double red_identity(int op)
 {
         return op == RED_SUM ? 0.0 : (op == RED_MAX ? -HUGE_VAL : HUGE_VAL);
@@ -44,6 +108,38 @@ __device__ __forceinline__ double red_combine(int op, double a, double b)
                 return (b > a) ? b : a;
         return (b < a) ? b : a;
 }
+
+__device__ __forceinline__ DF red_combine(int op, DF a, DF b)
+{
+        if (op == RED_SUM)
+                return df_add(a, b);
+        if (op == RED_MAX)
+                return (b.hi > a.hi) ? b : a;
+        return (b.hi < a.hi) ? b : a;
+}
+
+template <class P>
+__device__ __forceinline__ P red_identity_as(int op);
+template <>
+__device__ __forceinline__ double red_identity_as<double>(int op) { return red_identity(op); }
+template <>
+__device__ __forceinline__ DF red_identity_as<DF>(int op)
+{
+        float v = op == RED_SUM ? 0.f : (op == RED_MAX ? -HUGE_VALF : HUGE_VALF);
+        return {v, 0.f};
+}
+
+__device__ __forceinline__ double shfl_down(double v, int o)
+{
+        return __shfl_down_sync(0xffffffffu, v, o);
+}
+__device__ __forceinline__ DF shfl_down(DF v, int o)
+{
+        return {__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
+}
+
+__device__ __forceinline__ double to_double(double v) { return v; }
+__device__ __forceinline__ double to_double(DF v) { return (double)v.hi + (double)v.lo; }
 
 __device__ __forceinline__ unsigned long long global_ns()
 {
@@ -69,26 +165,28 @@ __device__ __forceinline__ int ld_acquire_int(const int * p)
 }
 
 // Lane 0 of each warp ends with the warp's combination (fixed tree order).
-__device__ __forceinline__ double warp_reduce(double v, int op)
+template <class P>
+__device__ __forceinline__ P warp_reduce(P v, int op)
 {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)
-                v = red_combine(op, v, __shfl_down_sync(0xffffffffu, v, o));
+                v = red_combine(op, v, shfl_down(v, o));
         return v;
 }
 
-// Block-wide reduction of K values; the totals land in out[0..K) (shared)
-// and are visible to every thread of the block on return.
-template <int K>
-__device__ __forceinline__ void block_reduce(double (&v)[K], const int (&op)[K],
+// Block-wide reduction of K partials (double or DF); the totals, as
+// doubles, land in out[0..K) (shared) and are visible to every thread of
+// the block on return.
+template <int K, class P>
+__device__ __forceinline__ void block_reduce(const P (&v)[K], const int (&op)[K],
                                              double * out)
 {
-        __shared__ double part[kWarp][kRedMax];
+        __shared__ P part[kWarp][kRedMax];
         int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         int nw = (blockDim.x + 31) >> 5;
 #pragma unroll
         for (int k = 0; k < K; k++) {
-                double r = warp_reduce(v[k], op[k]);
+                P r = warp_reduce(v[k], op[k]);
                 if (lane == 0)
                         part[warp][k] = r;
         }
@@ -96,11 +194,10 @@ __device__ __forceinline__ void block_reduce(double (&v)[K], const int (&op)[K],
         if (warp == 0) {
 #pragma unroll
                 for (int k = 0; k < K; k++) {
-                        double r = (lane < nw) ? part[lane][k]
-                                               : red_identity(op[k]);
+                        P r = (lane < nw) ? part[lane][k] : red_identity_as<P>(op[k]);
                         r = warp_reduce(r, op[k]);
                         if (lane == 0)
-                                out[k] = r;
+                                out[k] = to_double(r);
                 }
         }
         __syncthreads();
@@ -177,8 +274,8 @@ struct GridTeam {
         }
 
         // Reduction + barrier.  Returns false if the team has failed.
-        template <int K>
-        __device__ bool reduce(double (&v)[K], const int (&op)[K])
+        template <int K, class P>
+        __device__ bool reduce_to(const P (&v)[K], const int (&op)[K], double (&res)[K])
         {
                 __shared__ double tot[kRedMax];
                 __shared__ int bad;
@@ -276,10 +373,17 @@ struct GridTeam {
                 __syncthreads();
 #pragma unroll
                 for (int k = 0; k < K; k++)
-                        v[k] = tot[k];
+                        res[k] = tot[k];
                 int b = bad;
                 parity ^= 1;
                 return !b;
+        }
+
+        // In-place form for double partials.
+        template <int K>
+        __device__ bool reduce(double (&v)[K], const int (&op)[K])
+        {
+                return reduce_to<K, double>(v, op, v);
         }
 
         __device__ bool sync()
@@ -308,15 +412,22 @@ struct BlockTeam {
 
         // Failures of a one-CTA team are raised by its own threads, which
         // all return at once, so the reduction needs no status check.
-        template <int K>
-        __device__ bool reduce(double (&v)[K], const int (&op)[K])
+        template <int K, class P>
+        __device__ bool reduce_to(const P (&v)[K], const int (&op)[K], double (&res)[K])
         {
                 __shared__ double tot[kRedMax];
                 block_reduce<K>(v, op, tot);
 #pragma unroll
                 for (int k = 0; k < K; k++)
-                        v[k] = tot[k];
+                        res[k] = tot[k];
                 return true;
+        }
+
+        // In-place form for double partials.
+        template <int K>
+        __device__ bool reduce(double (&v)[K], const int (&op)[K])
+        {
+                return reduce_to<K, double>(v, op, v);
         }
 
         __device__ bool sync()
@@ -357,8 +468,8 @@ struct ClusterTeam {
 
         // Failures are decided from reduced values, identically in every CTA,
         // so the reduction needs no status check.
-        template <int K>
-        __device__ bool reduce(double (&v)[K], const int (&op)[K])
+        template <int K, class P>
+        __device__ bool reduce_to(const P (&v)[K], const int (&op)[K], double (&res)[K])
         {
                 __shared__ double part[2][kRedMax];
                 __shared__ double tot[kRedMax];
@@ -382,9 +493,16 @@ struct ClusterTeam {
                 __syncthreads();
 #pragma unroll
                 for (int k = 0; k < K; k++)
-                        v[k] = tot[k];
+                        res[k] = tot[k];
                 parity ^= 1;
                 return true;
+        }
+
+        // In-place form for double partials.
+        template <int K>
+        __device__ bool reduce(double (&v)[K], const int (&op)[K])
+        {
+                return reduce_to<K, double>(v, op, v);
         }
 
         __device__ bool sync()

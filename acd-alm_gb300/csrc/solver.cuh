@@ -126,15 +126,35 @@ __device__ __forceinline__ float lerp2(float a, float x, float b, float y)
 
 __device__ __forceinline__ bool is_nan(double v) { return v != v; }
 
+// Reduction partials of an inner solve: FP64 for the FP64 solve, float-float
+// for the FP32 one (its FP64 pipe work would otherwise bound the iteration).
+template <class T>
+struct AccOf {
+        typedef double type;
+};
+template <>
+struct AccOf<float> {
+        typedef DF type;
+};
+
+// NaN test on the bits (integer pipe).
+__device__ __forceinline__ bool nan_bits(double v)
+{
+        return (__double_as_longlong(v) & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
+}
+
 template <class T, class Team, bool Exact>
 struct Approx {
+        typedef typename AccOf<T>::type Acc;
         Team & tm;
         InnerProblem<T> P;
         InnerWork<T> W;
         LogBuf log;
         Vec<T> y, z, zp, x;
         long long iteration;
-        double theta, step_length;
+        // momentum and step length: in T (the FP32 solve only ever uses them
+        // rounded to float)
+        T theta, step_length;
         int restarts_since_log;
         bool ok;
         unsigned long long t_start_ns;
@@ -148,6 +168,12 @@ struct Approx {
         }
 
         __device__ int lane() const { return threadIdx.x & 31; }
+
+        template <int K>
+        __device__ bool reduce(const Acc (&part)[K], const int (&op)[K], double (&res)[K])
+        {
+                return tm.template reduce_to<K, Acc>(part, op, res);
+        }
 
         __device__ void put_log(const LogRec & r)
         {
@@ -166,13 +192,13 @@ struct Approx {
         // (1-nth) x_viol + nth v_viol); 2 = the same into the spare buffers
         // (the caller keeps them only if the line search accepts).  Optional
         // n-vector partials of v.x: c'v (value), |v|^2 and |prev - v|^2.
-        __device__ bool violation(Vec<T> & v, int linterp, double th, double nth,
+        __device__ bool violation(Vec<T> & v, int linterp, T th, T nth,
                                   bool want_cx, bool want_delta, double * cx,
                                   double * xx, double * dd2, double * elapsed = nullptr)
         {
-                double part[5] = {0, 0, 0, 0, 0};
+                Acc part[5] = {};
                 const int op[5] = {RED_SUM, RED_SUM, RED_SUM, RED_SUM, RED_MAX};
-                const T ts = (T)(1 - th), tt = (T)th, ns = (T)(1 - nth), nt = (T)nth;
+                const T ts = T(1) - th, tt = th, ns = T(1) - nth, nt = nth;
                 T * xvw = (linterp == 2) ? W.alt_xv : x.viol;
                 T * yvw = (linterp == 2) ? W.alt_yv : y.viol;
                 T * xxw = (linterp == 2) ? W.alt_x : x.x;
@@ -182,7 +208,7 @@ struct Approx {
                         T r = ax - tm.ld(P.b + i);
                         T s = mul<Exact>(tm.ld(P.w + i), r);
                         v.viol[i] = s;
-                        part[0] += (double)s * (double)r;
+                        acc_prod(part[0], s, r);
                         if (linterp) {
                                 T xv = lerp2<Exact>(ts, tm.ld(xvr + i), tt, s);
                                 yvw[i] = lerp2<Exact>(ns, xv, nt, s);
@@ -195,29 +221,30 @@ struct Approx {
                                 if (linterp)
                                         xxw[j] = lerp2<Exact>(ts, tm.ld(xxr + j), tt, vj);
                                 if (want_cx)
-                                        part[1] += (double)tm.ld(P.c + j) * (double)vj;
+                                        acc_prod(part[1], tm.ld(P.c + j), vj);
                                 if (want_delta) {
                                         double d = (double)tm.ld(W.prev + j) - (double)vj;
                                         double full = xbar ? xbar[j] + (double)vj : (double)vj;
-                                        part[2] += full * full;
-                                        part[3] += d * d;
+                                        acc_add(part[2], full * full);
+                                        acc_add(part[3], d * d);
                                 }
                         }
                 }
                 if (elapsed)
-                        part[4] = (double)(global_ns() - t_start_ns);
-                if (!tm.reduce(part, op))
+                        acc_max(part[4], (T)(global_ns() - t_start_ns));
+                double res[5];
+                if (!reduce(part, op, res))
                         return false;
-                v.quad = .5 * part[0];
+                v.quad = .5 * res[0];
                 v.violp = 1;
                 if (elapsed)
-                        *elapsed = part[4];
+                        *elapsed = res[4];
                 if (cx)
-                        *cx = part[1];
+                        *cx = res[1];
                 if (xx)
-                        *xx = part[2];
+                        *xx = res[2];
                 if (dd2)
-                        *dd2 = part[3];
+                        *dd2 = res[3];
                 return true;
         }
 
@@ -231,14 +258,14 @@ struct Approx {
         struct StepOut {
                 double maxz, est, pg2, dd, cz, czp;
         };
-        __device__ bool at_step(bool two, bool is_long, double itheta, double theta2,
+        __device__ bool at_step(bool two, bool is_long, T itheta, T theta2,
                                 bool want_pg, bool want_dd, bool want_cz,
                                 StepOut & o)
         {
-                double part[6] = {0, 0, 0, 0, 0, 0};
+                Acc part[6] = {};
                 const int op[6] = {is_long ? RED_SUM : RED_MAX, RED_SUM, RED_SUM,
                                    RED_SUM, RED_SUM, RED_SUM};
-                const T it = (T)itheta, t2 = (T)theta2;
+                const T it = itheta, t2 = theta2;
                 T * g = W.g;
                 T * g2 = W.g2;
                 auto epi = [&](int j, T g0, T g1) {
@@ -258,39 +285,38 @@ struct Approx {
                         zp.x[j] = trial;
                         T delta = trial - zj;
                         if (is_long) {
-                                part[0] += (double)g1 * (double)delta;
-                                part[1] += (double)delta * (double)delta
-                                        * (double)t2 * (double)tm.ld(P.v + j);
+                                acc_prod(part[0], g1, delta);
+                                acc_add(part[1], delta * delta * t2 * tm.ld(P.v + j));
                         } else {
-                                double a = fabs((double)trial);
-                                part[0] = (a > part[0]) ? a : part[0];
+                                acc_max(part[0], fabs(trial));
                         }
                         if (want_pg) {
                                 T xp = zj - g0;
                                 xp = maxpd(lj, xp);
                                 xp = minpd(uj, xp);
-                                double d = (double)zj - (double)xp;
-                                part[2] += d * d;
+                                T d = zj - xp;
+                                acc_prod(part[2], d, d);
                         }
                         if (want_dd)
-                                part[3] += (double)g0 * (double)delta;
+                                acc_prod(part[3], g0, delta);
                         if (want_cz)
-                                part[4] += (double)cj * (double)zj;
-                        part[5] += (double)cj * (double)trial;
+                                acc_prod(part[4], cj, zj);
+                        acc_prod(part[5], cj, trial);
                 };
                 if (two)
                         sell_rows_2<Exact>(tm, P.At, z.viol, y.viol, epi);
                 else
                         sell_rows_1<Exact>(tm, P.At, y.viol,
                                            [&](int j, T g1) { epi(j, (T)0, g1); });
-                if (!tm.reduce(part, op))
+                double res[6];
+                if (!reduce(part, op, res))
                         return false;
-                o.maxz = is_long ? 0 : part[0];
-                o.est = is_long ? part[0] + .5 * part[1] : 0;
-                o.pg2 = part[2];
-                o.dd = part[3];
-                o.cz = part[4];
-                o.czp = part[5];
+                o.maxz = is_long ? 0 : res[0];
+                o.est = is_long ? res[0] + .5 * res[1] : 0;
+                o.pg2 = res[2];
+                o.dd = res[3];
+                o.cz = res[4];
+                o.czp = res[5];
                 return true;
         }
 
@@ -300,7 +326,7 @@ struct Approx {
         __device__ bool gradient(const Vec<T> & v, bool copy_prev, double & pg2,
                                  double & gg)
         {
-                double part[2] = {0, 0};
+                Acc part[2] = {};
                 const int op[2] = {RED_SUM, RED_SUM};
                 T * g = W.g;
                 sell_rows_1<Exact>(tm, P.At, v.viol, [&](int j, T a) {
@@ -310,16 +336,17 @@ struct Approx {
                         T xp = xj - gj;
                         xp = maxpd(tm.ld(P.l + j), xp);
                         xp = minpd(tm.ld(P.u + j), xp);
-                        double d = (double)xj - (double)xp;
-                        part[0] += d * d;
-                        part[1] += (double)gj * (double)gj;
+                        T d = xj - xp;
+                        acc_prod(part[0], d, d);
+                        acc_prod(part[1], gj, gj);
                         if (copy_prev)
                                 W.prev_alt[j] = xj;
                 });
-                if (!tm.reduce(part, op))
+                double res[2];
+                if (!reduce(part, op, res))
                         return false;
-                pg2 = part[0];
-                gg = part[1];
+                pg2 = res[0];
+                gg = res[1];
                 return true;
         }
 
@@ -329,9 +356,9 @@ struct Approx {
         // dot_diff (approx.c:227-256) on the new zp.
         __device__ bool retry_step(bool need_grad, double & dd)
         {
-                double part[1] = {0};
+                Acc part[1] = {};
                 const int op[1] = {RED_SUM};
-                const T it = (T)((1 - 1e-6) / theta);
+                const T it = T(1 - 1e-6) / theta;
                 T * g = W.g;
                 auto body = [&](int j, T gj) {
                         T zj = tm.ld(z.x + j);
@@ -340,7 +367,7 @@ struct Approx {
                         trial = maxpd(tm.ld(P.l + j), trial);
                         trial = minpd(tm.ld(P.u + j), trial);
                         zp.x[j] = trial;
-                        part[0] += (double)gj * ((double)trial - (double)zj);
+                        acc_prod(part[0], gj, trial - zj);
                 };
                 if (need_grad) {
                         sell_rows_1<Exact>(tm, P.At, z.viol, [&](int j, T a) {
@@ -352,9 +379,10 @@ struct Approx {
                         for (int j = tm.tid(); j < P.n; j += tm.nthreads())
                                 body(j, tm.ld(g + j));
                 }
-                if (!tm.reduce(part, op))
+                double res[1];
+                if (!reduce(part, op, res))
                         return false;
-                dd = part[0];
+                dd = res[0];
                 return true;
         }
 
@@ -378,22 +406,23 @@ struct Approx {
         // (gradient_value.inc:111-133).
         __device__ bool value_of(Vec<T> & v, double & out)
         {
-                if (!is_nan(v.value)) {
+                if (!nan_bits(v.value)) {
                         out = v.value;
                         return true;
                 }
                 double cx = 0;
-                if (is_nan(v.quad) || !v.violp) {
+                if (nan_bits(v.quad) || !v.violp) {
                         if (!violation(v, 0, 0, 0, true, false, &cx, nullptr, nullptr))
                                 return false;
                 } else {
-                        double part[1] = {0};
+                        Acc part[1] = {};
                         const int op[1] = {RED_SUM};
                         for (int j = tm.tid(); j < P.n; j += tm.nthreads())
-                                part[0] += (double)tm.ld(P.c + j) * (double)tm.ld(v.x + j);
-                        if (!tm.reduce(part, op))
+                                acc_prod(part[0], tm.ld(P.c + j), tm.ld(v.x + j));
+                        double res[1];
+                        if (!reduce(part, op, res))
                                 return false;
-                        cx = part[0];
+                        cx = res[0];
                 }
                 v.value = v.quad + cx;
                 out = v.value;
@@ -402,33 +431,35 @@ struct Approx {
 
         __device__ bool norms_vs_prev(const Vec<T> & v, double & xx, double & dd2)
         {
-                double part[2] = {0, 0};
+                Acc part[2] = {};
                 const int op[2] = {RED_SUM, RED_SUM};
                 for (int j = tm.tid(); j < P.n; j += tm.nthreads()) {
                         double vj = (double)tm.ld(v.x + j);
                         double d = (double)tm.ld(W.prev + j) - vj;
                         double full = xbar ? xbar[j] + vj : vj;
-                        part[0] += full * full;
-                        part[1] += d * d;
+                        acc_add(part[0], full * full);
+                        acc_add(part[1], d * d);
                 }
-                if (!tm.reduce(part, op))
+                double res[2];
+                if (!reduce(part, op, res))
                         return false;
-                xx = part[0];
-                dd2 = part[1];
+                xx = res[0];
+                dd2 = res[1];
                 return true;
         }
 
         __device__ bool norm_g(double & gg)
         {
-                double part[1] = {0};
+                Acc part[1] = {};
                 const int op[1] = {RED_SUM};
                 for (int j = tm.tid(); j < P.n; j += tm.nthreads()) {
-                        double gj = (double)tm.ld(W.g + j);
-                        part[0] += gj * gj;
+                        T gj = tm.ld(W.g + j);
+                        acc_prod(part[0], gj, gj);
                 }
-                if (!tm.reduce(part, op))
+                double res[1];
+                if (!reduce(part, op, res))
                         return false;
-                gg = part[0];
+                gg = res[0];
                 return true;
         }
 
@@ -453,17 +484,17 @@ struct Approx {
         __device__ int iter(bool want_pg, double & out_pg)
         {
                 bool descent, got_gradient;
-                double stepl = step_length;
+                T stepl = step_length;
                 double dd = 0;
                 bool dd_valid = false;
                 bool spec_valid = false;  // alt buffers hold linterp of zp
-                double th = theta;
-                double nth = 2.0 / ((double)(iteration + 1) + 2);
+                T th = theta;
+                T nth = T(2) / ((T)(iteration + 1) + T(2));
                 if (stepl <= 1) {
                         // short_step, approx.c:394-415
                         StepOut o;
-                        bool want_cz = is_nan(z.value);
-                        if (!at_step(true, false, (1 - 1e-6) / th, 0, want_pg, true,
+                        bool want_cz = nan_bits(z.value);
+                        if (!at_step(true, false, T(1 - 1e-6) / th, T(0), want_pg, true,
                                      want_cz, o))
                                 return -1;
                         if (!check_finite(o.maxz))
@@ -471,9 +502,9 @@ struct Approx {
                         if (want_cz)
                                 z.value = z.quad + o.cz;
                         invalidate(zp);
-                        step_length = stepl * 1.01;
-                        if (step_length > 1)
-                                step_length = 1 + 1e-6;
+                        step_length = stepl * T(1.01);
+                        if (step_length > T(1))
+                                step_length = T(1 + 1e-6);
                         descent = false;
                         got_gradient = true;
                         dd = o.dd;
@@ -482,12 +513,12 @@ struct Approx {
                                 out_pg = sqrt(o.pg2);
                 } else {
                         // try_long_step, approx.c:343-392
-                        got_gradient = want_pg || (stepl <= 1 + 1e-6);
-                        bool safe = (stepl <= 1 + 1e-6);
-                        double len = safe ? 1.0 : stepl;
+                        got_gradient = want_pg || (stepl <= T(1 + 1e-6));
+                        bool safe = (stepl <= T(1 + 1e-6));
+                        T len = safe ? T(1) : stepl;
                         StepOut o;
-                        bool want_cz = is_nan(z.value);
-                        if (!at_step(got_gradient, true, (len - 1e-6) / th, th / len,
+                        bool want_cz = nan_bits(z.value);
+                        if (!at_step(got_gradient, true, (len - T(1e-6)) / th, th / len,
                                      want_pg, got_gradient, want_cz, o))
                                 return -1;
                         if (want_cz)
@@ -509,10 +540,10 @@ struct Approx {
                                 dd_valid = true;
                         }
                         if (now <= initial + o.est) {
-                                step_length = len * 1.01;
+                                step_length = len * T(1.01);
                                 descent = true;
                         } else {
-                                step_length = .9 * len;
+                                step_length = T(.9) * len;
                                 descent = false;
                                 if (!safe) {
                                         if (!retry_step(!got_gradient, dd))

@@ -156,6 +156,14 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned * p)
         return v;
 }
 
+__device__ __forceinline__ int ld_relaxed_int(const int * p)
+{
+        int v;
+        asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p)
+                     : "memory");
+        return v;
+}
+
 __device__ __forceinline__ int ld_acquire_int(const int * p)
 {
         int v;
@@ -342,6 +350,11 @@ struct GridTeam {
                 // warp k sums value k over all CTAs: each lane first issues all
                 // its loads (CTAs lane, lane+32, ...), then combines them in
                 // that fixed order, then a fixed shuffle tree
+                // the team's status word is read alongside the values (a
+                // relaxed load: it only has to show a failure eventually)
+                int status_now = 0;
+                if (threadIdx.x == 0)
+                        status_now = ld_relaxed_int(status());
                 {
                         int lane = threadIdx.x & 31, wk = threadIdx.x >> 5;
 #pragma unroll
@@ -369,7 +382,7 @@ struct GridTeam {
                         }
                 }
                 if (threadIdx.x == 0)
-                        bad = ld_acquire_int(status()) != 0;
+                        bad = status_now != 0;
                 __syncthreads();
 #pragma unroll
                 for (int k = 0; k < K; k++)
@@ -537,18 +550,22 @@ struct Slice {
         bool lead;      // this lane owns its row's result
 };
 
-template <class V>
-__device__ __forceinline__ Slice slice_of(const SellDev<V> & op, int s, int lane)
+__device__ __forceinline__ Slice slice_from(int64_t p0, int64_t p1, int row0, int lane)
 {
         Slice sl;
-        int64_t p0 = __ldg(op.ptr + s), p1 = __ldg(op.ptr + s + 1);
         sl.shift = (int)(p0 & 7);
         sl.vec = (p0 & 8) != 0;
         sl.base = p0 & ~int64_t(31);
         sl.steps = (int)(((p1 & ~int64_t(31)) - sl.base) >> (sl.vec ? 7 : 5));
-        sl.row = __ldg(op.row0 + s) + (lane >> sl.shift);
+        sl.row = row0 + (lane >> sl.shift);
         sl.lead = (lane & ((1 << sl.shift) - 1)) == 0;
         return sl;
+}
+
+template <class V>
+__device__ __forceinline__ Slice slice_of(const SellDev<V> & op, int s, int lane)
+{
+        return slice_from(__ldg(op.ptr + s), __ldg(op.ptr + s + 1), __ldg(op.row0 + s), lane);
 }
 
 // Entries per lane per step, as a type (for generic lambdas).
@@ -618,6 +635,43 @@ __device__ __forceinline__ void for_each_slice(const Team & tm, int nslices, F &
                         break;
                 if (s < nslices)
                         f(s);
+        }
+}
+
+// The same walk over the slices of one operator, handing f the decoded
+// slice; the next slice's words are loaded while f works on the current
+// one (a warp handles only a few slices per pass, so the load latency of
+// each slice's header would otherwise be exposed).
+template <class Team, class V, class F>
+__device__ __forceinline__ void for_each_slice_of(const Team & tm, const SellDev<V> & op,
+                                                  int lane, F && f)
+{
+        int w = tm.warp(), W = tm.nwarps();
+        const int ns = op.nslices;
+        auto pick = [&](int round) { return round * W + ((round & 1) ? W - 1 - w : w); };
+        int s = pick(0);
+        int64_t p0 = 0, p1 = 0;
+        int r0 = 0;
+        if (s < ns) {
+                p0 = __ldg(op.ptr + s);
+                p1 = __ldg(op.ptr + s + 1);
+                r0 = __ldg(op.row0 + s);
+        }
+        for (int round = 0; round * W < ns; round++) {
+                int sn = pick(round + 1);
+                int64_t q0 = 0, q1 = 0;
+                int rn = 0;
+                if (sn < ns) {
+                        q0 = __ldg(op.ptr + sn);
+                        q1 = __ldg(op.ptr + sn + 1);
+                        rn = __ldg(op.row0 + sn);
+                }
+                if (s < ns)
+                        f(slice_from(p0, p1, r0, lane));
+                s = sn;
+                p0 = q0;
+                p1 = q1;
+                r0 = rn;
         }
 }
 
@@ -738,31 +792,50 @@ __device__ __forceinline__ T slice_row_sum(const Team & tm, const SellDev<V> & o
         }
 }
 
+// Row sums of one SELL operator applied to x.  For every live row, in the
+// row's lead lane: pv = pre(row) is loaded before the row's entries (so the
+// epilogue's operands arrive while the row is summed), then
+// epi(row, sum, pv).
+template <bool Exact, class Team, class V, class T, class Pre, class Epi>
+__device__ __forceinline__ void sell_rows_1p(const Team & tm, const SellDev<V> & op,
+                                             const T * x, Pre && pre, Epi && epi)
+{
+        int lane = threadIdx.x & 31;
+        for_each_slice_of(tm, op, lane, [&](const Slice & sl) {
+                bool live = sl.lead && sl.row < op.nrows;
+                auto pv = pre(live ? sl.row : -1);
+                T acc = by_width(sl, [&](auto w) {
+                        return slice_row_sum<Exact, decltype(w)::value>(tm, op, sl, x, lane);
+                });
+                if (live)
+                        epi(sl.row, acc, pv);
+        });
+}
+
+struct NoPre {
+        __device__ int operator()(int) const { return 0; }
+};
+
 // Row sums of one SELL operator applied to x; calls epi(row, sum) in the
 // row's lead lane for every live row.
 template <bool Exact, class Team, class V, class T, class Epi>
 __device__ __forceinline__ void sell_rows_1(const Team & tm, const SellDev<V> & op,
                                             const T * x, Epi && epi)
 {
-        int lane = threadIdx.x & 31;
-        for_each_slice(tm, op.nslices, [&](int s) {
-                Slice sl = slice_of(op, s, lane);
-                T acc = by_width(sl, [&](auto w) {
-                        return slice_row_sum<Exact, decltype(w)::value>(tm, op, sl, x, lane);
-                });
-                if (sl.lead && sl.row < op.nrows)
-                        epi(sl.row, acc);
-        });
+        sell_rows_1p<Exact>(tm, op, x, NoPre(), [&](int r, T acc, int) { epi(r, acc); });
 }
 
-// Two right-hand sides sharing one pass over the operator.
-template <bool Exact, class Team, class V, class T, class Epi>
-__device__ __forceinline__ void sell_rows_2(const Team & tm, const SellDev<V> & op,
-                                            const T * x0, const T * x1, Epi && epi)
+// Two right-hand sides sharing one pass over the operator, with the same
+// pre / epi protocol as sell_rows_1p: epi(row, sum0, sum1, pv).
+template <bool Exact, class Team, class V, class T, class Pre, class Epi>
+__device__ __forceinline__ void sell_rows_2p(const Team & tm, const SellDev<V> & op,
+                                             const T * x0, const T * x1, Pre && pre,
+                                             Epi && epi)
 {
         int lane = threadIdx.x & 31;
-        for_each_slice(tm, op.nslices, [&](int s) {
-                Slice sl = slice_of(op, s, lane);
+        for_each_slice_of(tm, op, lane, [&](const Slice & sl) {
+                bool live = sl.lead && sl.row < op.nrows;
+                auto pv = pre(live ? sl.row : -1);
                 T a0 = 0, a1 = 0;
                 by_width(sl, [&](auto w) {
                         constexpr int VEC = decltype(w)::value;
@@ -798,9 +871,17 @@ __device__ __forceinline__ void sell_rows_2(const Team & tm, const SellDev<V> & 
                         }
                         return 0;
                 });
-                if (sl.lead && sl.row < op.nrows)
-                        epi(sl.row, a0, a1);
+                if (live)
+                        epi(sl.row, a0, a1, pv);
         });
+}
+
+template <bool Exact, class Team, class V, class T, class Epi>
+__device__ __forceinline__ void sell_rows_2(const Team & tm, const SellDev<V> & op,
+                                            const T * x0, const T * x1, Epi && epi)
+{
+        sell_rows_2p<Exact>(tm, op, x0, x1, NoPre(),
+                            [&](int r, T a0, T a1, int) { epi(r, a0, a1); });
 }
 
 }  // namespace acd

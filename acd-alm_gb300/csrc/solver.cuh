@@ -204,13 +204,26 @@ struct Approx {
                 T * xxw = (linterp == 2) ? W.alt_x : x.x;
                 const T * xvr = x.viol;
                 const T * xxr = x.x;
-                sell_rows_1<Exact>(tm, P.A, v.x, [&](int i, T ax) {
-                        T r = ax - tm.ld(P.b + i);
-                        T s = mul<Exact>(tm.ld(P.w + i), r);
+                struct RowPre {
+                        T b, w, xv;
+                };
+                auto pre = [&](int i) {
+                        RowPre q = {T(0), T(0), T(0)};
+                        if (i >= 0) {
+                                q.b = tm.ld(P.b + i);
+                                q.w = tm.ld(P.w + i);
+                                if (linterp)
+                                        q.xv = tm.ld(xvr + i);
+                        }
+                        return q;
+                };
+                sell_rows_1p<Exact>(tm, P.A, v.x, pre, [&](int i, T ax, const RowPre & q) {
+                        T r = ax - q.b;
+                        T s = mul<Exact>(q.w, r);
                         v.viol[i] = s;
                         acc_prod(part[0], s, r);
                         if (linterp) {
-                                T xv = lerp2<Exact>(ts, tm.ld(xvr + i), tt, s);
+                                T xv = lerp2<Exact>(ts, q.xv, tt, s);
                                 yvw[i] = lerp2<Exact>(ns, xv, nt, s);
                                 xvw[i] = xv;
                         }
@@ -268,17 +281,33 @@ struct Approx {
                 const T it = itheta, t2 = theta2;
                 T * g = W.g;
                 T * g2 = W.g2;
-                auto epi = [&](int j, T g0, T g1) {
-                        T cj = tm.ld(P.c + j);
+                struct ColPre {
+                        T c, z, l, u, iv, v;
+                };
+                auto pre = [&](int j) {
+                        ColPre q = {T(0), T(0), T(0), T(0), T(0), T(0)};
+                        if (j >= 0) {
+                                q.c = tm.ld(P.c + j);
+                                q.z = tm.ld(z.x + j);
+                                q.l = tm.ld(P.l + j);
+                                q.u = tm.ld(P.u + j);
+                                q.iv = tm.ld(P.inv_v + j);
+                                if (is_long)
+                                        q.v = tm.ld(P.v + j);
+                        }
+                        return q;
+                };
+                auto epi = [&](int j, T g0, T g1, const ColPre & q) {
+                        T cj = q.c;
                         if (two)
                                 g0 = g0 + cj;
                         g1 = g1 + cj;
                         if (two)
                                 g[j] = g0;
                         g2[j] = g1;
-                        T zj = tm.ld(z.x + j);
-                        T lj = tm.ld(P.l + j), uj = tm.ld(P.u + j);
-                        T stp = mul<Exact>(it, tm.ld(P.inv_v + j));
+                        T zj = q.z;
+                        T lj = q.l, uj = q.u;
+                        T stp = mul<Exact>(it, q.iv);
                         T trial = msub<Exact>(zj, g1, stp);
                         trial = maxpd(lj, trial);
                         trial = minpd(uj, trial);
@@ -286,7 +315,7 @@ struct Approx {
                         T delta = trial - zj;
                         if (is_long) {
                                 acc_prod(part[0], g1, delta);
-                                acc_add(part[1], delta * delta * t2 * tm.ld(P.v + j));
+                                acc_add(part[1], delta * delta * t2 * q.v);
                         } else {
                                 acc_max(part[0], fabs(trial));
                         }
@@ -304,10 +333,12 @@ struct Approx {
                         acc_prod(part[5], cj, trial);
                 };
                 if (two)
-                        sell_rows_2<Exact>(tm, P.At, z.viol, y.viol, epi);
+                        sell_rows_2p<Exact>(tm, P.At, z.viol, y.viol, pre, epi);
                 else
-                        sell_rows_1<Exact>(tm, P.At, y.viol,
-                                           [&](int j, T g1) { epi(j, (T)0, g1); });
+                        sell_rows_1p<Exact>(tm, P.At, y.viol, pre,
+                                            [&](int j, T g1, const ColPre & q) {
+                                                    epi(j, (T)0, g1, q);
+                                            });
                 double res[6];
                 if (!reduce(part, op, res))
                         return false;

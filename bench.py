@@ -196,6 +196,10 @@ def cpu_baseline(lp, gpu_inner_per_lp: float, iters: int, threads: int):
     dt = time.perf_counter() - t0
     lib.approx_free(a)
     lib.matrix_free(m)
+    # iterations actually run (diag[4], approx.c:681-702); min_delta = 0 and
+    # max_pg = 0 keep the loop going, this guards an early exit
+    done = int(diag[4]) if diag[4] > 0 else iters
+    iters = min(iters, done)
     per_iter = dt / max(iters, 1)
     return {"value": 1.0 / (per_iter * gpu_inner_per_lp), "unit": "LP/s",
             "cores": threads, "kind": kind,
@@ -254,7 +258,8 @@ def main():
     ap.add_argument("--profile-solve", type=int, default=0,
                     help="run one ALM solve capped at this many inner iterations and exit "
                          "(the command the ncu captures use)")
-    ap.add_argument("--ref-iters", type=int, default=200)
+    ap.add_argument("--ref-iters", type=int, default=8000,
+                    help="APPROX iterations each CPU sample times (about 10 s on 16 cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-side", action="store_true")
     ap.add_argument("--spmv", action="store_true",
@@ -296,6 +301,7 @@ def main():
         st = alm.stats()
         print(json.dumps({"profile_solve": args.profile_solve, "workload": args.workload,
                           "precision": args.precision, "inner": st["inner_iterations"],
+                          "inner32": st["fp32_inner_iterations"],
                           "device_seconds": st["seconds"]}))
         return
     L.acdalm_launch_count.restype = __import__("ctypes").c_ulonglong

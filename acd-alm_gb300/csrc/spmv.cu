@@ -297,6 +297,10 @@ int launch(sparse_matrix_t * a, int variant, int transpose, const T * x0,
            const T * x1, T * y0, T * y1, cudaStream_t s)
 {
         bool f32 = sizeof(T) == 4;
+        // the fused-rounding SELL product runs over the SELL layout
+        bool fused = variant == ACDALM_SPMV_SELL_FMA;
+        if (fused)
+                variant = ACDALM_SPMV_SELL;
         int r = ensure_layout(a, variant, transpose, f32);
         if (r)
                 return r;
@@ -306,12 +310,20 @@ int launch(sparse_matrix_t * a, int variant, int transpose, const T * x0,
         if (variant == ACDALM_SPMV_SELL) {
                 int blocks = grid_for((long long)L.sell.nslices * 32, 256);
                 if constexpr (sizeof(T) == 8) {
-                        if (x1)
+                        if (fused) {
+                                if (x1)
+                                        acd::sell2_kernel<double, false><<<blocks, 256, 0, s>>>(
+                                                L.sell, L.row_of_d, x0, x1, y0, y1);
+                                else
+                                        acd::sell_kernel<double, false><<<blocks, 256, 0, s>>>(
+                                                L.sell, L.row_of_d, x0, y0);
+                        } else if (x1) {
                                 acd::sell2_kernel<double, true><<<blocks, 256, 0, s>>>(
                                         L.sell, L.row_of_d, x0, x1, y0, y1);
-                        else
+                        } else {
                                 acd::sell_kernel<double, true><<<blocks, 256, 0, s>>>(
                                         L.sell, L.row_of_d, x0, y0);
+                        }
                 } else {
                         if (x1)
                                 acd::sell2_kernel<float, false><<<blocks, 256, 0, s>>>(
@@ -547,7 +559,7 @@ sparse_matrix_t * sparse_matrix_read(FILE * stream, int permute)
 int acdalm_spmv_variant(int variant)
 {
         int old = g_variant;
-        if (variant >= ACDALM_SPMV_SELL && variant <= ACDALM_SPMV_CSR)
+        if (variant >= ACDALM_SPMV_SELL && variant <= ACDALM_SPMV_SELL_FMA)
                 g_variant = variant;
         return old;
 }
@@ -556,7 +568,7 @@ int acdalm_spmv_device(const struct sparse_matrix * ca, int variant, int transpo
                        const double * x, double * y, void * stream)
 {
         sparse_matrix_t * a = const_cast<sparse_matrix_t *>(ca);
-        if (variant < 0 || variant > 2) {
+        if (variant < 0 || variant > ACDALM_SPMV_SELL_FMA) {
                 acd::set_error(ACDALM_EINVAL, "acdalm_spmv_device: variant %d", variant);
                 return ACDALM_EINVAL;
         }
@@ -569,7 +581,7 @@ int acdalm_spmv_device_f32(const struct sparse_matrix * ca, int variant, int tra
                            const float * x, float * y, void * stream)
 {
         sparse_matrix_t * a = const_cast<sparse_matrix_t *>(ca);
-        if (variant < 0 || variant > 2) {
+        if (variant < 0 || variant > ACDALM_SPMV_SELL_FMA) {
                 acd::set_error(ACDALM_EINVAL, "acdalm_spmv_device_f32: variant %d", variant);
                 return ACDALM_EINVAL;
         }
@@ -675,6 +687,8 @@ void preload_spmv_kernels()
         cudaFuncGetAttributes(&a, sell_kernel<float, false>);
         cudaFuncGetAttributes(&a, sell2_kernel<double, true>);
         cudaFuncGetAttributes(&a, sell2_kernel<float, false>);
+        cudaFuncGetAttributes(&a, sell_kernel<double, false>);
+        cudaFuncGetAttributes(&a, sell2_kernel<double, false>);
         cudaFuncGetAttributes(&a, block4_kernel<double>);
         cudaFuncGetAttributes(&a, csr_kernel<double, 4>);
         cudaFuncGetAttributes(&a, csr_kernel<double, 8>);

@@ -54,7 +54,120 @@ def workload(name: str):
         return inst.small()
     if name == "covering":
         return inst.covering()
+    if name in ("batch", "stream"):
+        return None
     raise SystemExit(f"unknown workload {name}")
+
+
+def _plain_fp64_rate(lib, lps):
+    """The plain FP64 GPU drop-in, one LP at a time (alm_solve on the whole
+    GPU): LPs/s over the given sample, from the solve kernels' device time."""
+    tot = 0.0
+    for lp in lps:
+        m = lib.Matrix(lp)
+        a = lib.Alm(m, lp)
+        a.set_kkt_tolerance(1e-6)
+        a.solve(1000)
+        tot += a.stats()["seconds"]
+        a.free()
+        m.free()
+    return len(lps) / tot
+
+
+def batch_bench(args):
+    """--workload batch: the 512-LP batch (m log-uniform in [200, 20000],
+    n = 2m, 6 nonzeros per column) in one persistent launch, one LP per CTA,
+    to 1e-6 relative KKT; FP64 and mixed forms, each against the plain FP64
+    drop-in solving a sample of the same LPs one at a time."""
+    lib = importlib.import_module("acd-alm_gb300.lib")
+    lps = inst.batch(args.batch_count)
+    mats = [lib.Matrix(lp) for lp in lps]
+    alms = [lib.Alm(m, lp) for m, lp in zip(mats, lps)]
+    L = lib.lib()
+    forms = []
+    for prec, name in ((0, "fp64"), (1, "mixed")):
+        for a, lp in zip(alms, lps):
+            a.set_kkt_tolerance(1e-6)
+            a.set_precision(prec)
+            w = np.ctypeslib.as_array(L.approx_weight(L.acdalm_alm_approx(a.h)), (lp.nrows,))
+            w[:] = 1.0
+        b = lib.Batch(alms)
+        ret, xs, lams, diag = b.solve(1000)
+        sec = b.seconds()
+        kk = [inst.rel_kkt(lps[i], xs[i], lams[i])["rel_kkt"]
+              for i in range(0, len(lps), max(1, len(lps) // 16))]
+        forms.append({"precision": name, "value": len(lps) / sec, "device_s": sec,
+                      "solved": int((ret == 0).sum()), "rel_kkt_host_sample_max": max(kk)})
+        b.free()
+    sample = [lps[i] for i in range(0, len(lps), max(1, len(lps) // args.plain_sample))]
+    plain = _plain_fp64_rate(lib, sample)
+    for a in alms:
+        a.free()
+    for m in mats:
+        m.free()
+    best = max(forms, key=lambda f: f["value"])
+    print(json.dumps({"metric": "LPs/sec to 1e-6 relative KKT (batch)", "value": best["value"],
+                      "unit": "LP/s", "n_gpus": 1, "higher_is_better": True,
+                      "dtype": "f64" if best["precision"] == "fp64" else "f32+f64",
+                      "data": "synthetic",
+                      "config": {"workload": f"batch of {len(lps)} LPs",
+                                 "m": "log-uniform [200, 20000]", "n": "2m",
+                                 "nnz_total": int(sum(lp.nnz for lp in lps))},
+                      "forms": forms,
+                      "plain_fp64_one_at_a_time": {"value": plain, "sample": len(sample)},
+                      "vs_plain_fp64": best["value"] / plain}), flush=True)
+
+
+def stream_bench(args):
+    """--workload stream: the first --stream-count requests of the served
+    stream (m log-uniform in [500, 200000], Poisson arrivals at 2000/s)
+    through the continuous-batching server; LPs/s over the wall time from
+    the first arrival to the last result, p50 / p99 latency (submission to
+    completion), against the plain FP64 drop-in one at a time on a sample."""
+    import threading
+    lib = importlib.import_module("acd-alm_gb300.lib")
+    arrivals, sizes, seeds = inst.stream_schedule()
+    k = args.stream_count
+    arrivals, sizes, seeds = arrivals[:k], sizes[:k], seeds[:k]
+    lps = [inst.batch_instance(int(m), int(sd)) for m, sd in zip(sizes, seeds)]
+    prec = 0 if args.precision == "fp64" else 1
+    srv = lib.Server(precision=prec, kkt_tol=1e-6)
+    t0 = time.perf_counter()
+    sub = {}
+
+    def submitter():
+        for i, lp in enumerate(lps):
+            now = time.perf_counter() - t0
+            if arrivals[i] > now:
+                time.sleep(arrivals[i] - now)
+            sub[srv.submit(lp)] = i
+
+    th = threading.Thread(target=submitter)
+    th.start()
+    done = {}
+    while len(done) < k and time.perf_counter() - t0 < args.stream_limit:
+        for rid in srv.poll(timeout=0.5):
+            done[rid] = srv.result(rid)
+    wall = time.perf_counter() - t0
+    th.join()
+    srv.close()
+    lat = np.array([v[4] for v in done.values()])
+    kk = [v[3]["rel_kkt"] for v in done.values()]
+    sample = [lps[i] for i in range(0, k, max(1, k // args.plain_sample))]
+    plain = _plain_fp64_rate(lib, sample)
+    rate = len(done) / wall
+    print(json.dumps({"metric": "LPs/sec and p50/p99 latency to 1e-6 relative KKT (stream)",
+                      "value": rate, "unit": "LP/s", "n_gpus": 1, "higher_is_better": True,
+                      "dtype": "f64" if prec == 0 else "f32+f64", "data": "synthetic",
+                      "config": {"workload": f"first {k} requests of the served stream",
+                                 "m": "log-uniform [500, 200000]", "n": "2m",
+                                 "arrivals": "Poisson 2000/s", "max_m": int(sizes.max())},
+                      "completed": len(done), "solved": sum(1 for v in done.values() if v[0] == 0),
+                      "wall_s": wall, "p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
+                      "p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
+                      "rel_kkt_device_max": max(kk) if kk else None,
+                      "plain_fp64_one_at_a_time": {"value": plain, "sample": len(sample)},
+                      "vs_plain_fp64": rate / plain}), flush=True)
 
 
 def spmv_bench(args, lp):
@@ -68,12 +181,12 @@ def spmv_bench(args, lp):
     stream = torch.cuda.current_stream()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     peak, peak_kind = load_peaks()
-    names = {0: "sell", 1: "block", 2: "csr"}
+    names = {0: "sell", 1: "block", 2: "csr", 3: "sell_fma"}
     out = []
-    for variant in (0, 2, 1):
+    for variant in (0, 3, 2, 1):
         for t in (0, 1):
             for f32 in (False, True):
-                if variant == 1 and f32:
+                if variant in (1, 3) and f32:
                     continue
                 dt = torch.float32 if f32 else torch.float64
                 nx, ny = (lp.nrows, lp.ncols) if t else (lp.ncols, lp.nrows)
@@ -239,6 +352,13 @@ def run_reference(args, lp, rank: int):
 
 METRIC = "LPs/sec to 1e-6 relative KKT"
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one FP32 inner
+# iteration of the mid LP's solve kernel, from one ncu capture of
+# `bench.py --profile-solve 3000` (3,000 FP32 iterations; see
+# profiles/alm_kernel_mid_traffic.md).  FP64 iterations are scaled by their
+# algorithmic bytes.
+MID_DRAM_BYTES_PER_FP32_ITER = (7724266240 + 3569961216) / 3000
+
 
 def config_of(args, lp):
     return {"workload": f"{args.workload} LP", "m": lp.nrows, "n": lp.ncols, "nnz": lp.nnz,
@@ -265,6 +385,12 @@ def main():
     ap.add_argument("--spmv", action="store_true",
                     help="time the device SpMV variants on the workload's matrix")
     ap.add_argument("--spmv-reps", type=int, default=10)
+    ap.add_argument("--batch-count", type=int, default=512)
+    ap.add_argument("--stream-count", type=int, default=48)
+    ap.add_argument("--stream-limit", type=float, default=900.0,
+                    help="seconds after which the stream run stops collecting")
+    ap.add_argument("--plain-sample", type=int, default=8,
+                    help="LPs the plain FP64 comparison solves one at a time")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -278,6 +404,12 @@ def main():
 
     if args.spmv:
         spmv_bench(args, lp)
+        return
+    if args.workload == "batch":
+        batch_bench(args)
+        return
+    if args.workload == "stream":
+        stream_bench(args)
         return
 
     import torch
@@ -375,6 +507,10 @@ def main():
     algo_bytes = mean_inner32 * bpi32 + (mean_inner - mean_inner32) * bpi
     achieved = algo_bytes / (tot_dev / args.steps) / 1e9
     peak, peak_kind = load_peaks()
+    traffic = None
+    if args.workload == "mid" and fp32:
+        traffic = MID_DRAM_BYTES_PER_FP32_ITER * (
+            mean_inner32 + (mean_inner - mean_inner32) * bpi / bpi32)
     line = {
         "metric": METRIC, "value": value, "unit": "LP/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
@@ -386,7 +522,10 @@ def main():
                 "h2d_bytes_per_step": 8 * (3 * lp.nrows + 4 * lp.ncols + lp.nrows + lp.ncols),
                 "d2h_bytes_per_step": 8 * (2 * lp.ncols + 2 * lp.nrows)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                     "traffic_note": "ncu DRAM bytes per launch, scaled from a 3,000-iteration "
+                                     "capture; the instance stays in L2, so traffic is far "
+                                     "below the algorithmic bytes",
                      "kernel": "alm_kernel (persistent cooperative solve)",
                      "peak_source": peak_kind,
                      "bytes_per_inner_iteration": {"fp64": bpi, "fp32": bpi32}},

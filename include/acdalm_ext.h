@@ -37,6 +37,10 @@ int acdalm_take_error(void);
 #define ACDALM_SPMV_SELL 0  /* warp-sliced ELL, 32 rows per slice (default) */
 #define ACDALM_SPMV_BLOCK 1 /* the 4-row block arena of the reference */
 #define ACDALM_SPMV_CSR 2   /* CSR, a sub-warp per row */
+/* SELL with fused multiply-adds and a lane tree per row: not bit-identical
+ * to the reference (within 1e-12 relative), but not bound by the FP64
+ * issue rate the separately rounded product needs. */
+#define ACDALM_SPMV_SELL_FMA 3
 /* Variant used by sparse_matrix_multiply{,_2}; returns the previous one. */
 int acdalm_spmv_variant(int variant);
 /* y = op(A) x with x and y already in device memory, launched on `stream`

@@ -1,7 +1,8 @@
 """Device SpMV parity (spmv.c:159-233, spmv_block.c:160-320): the SELL and
 block variants add each row in the reference's order with the reference's
 rounding, so they match the oracle (the reference restated) bit for bit;
-the CSR variant re-associates and is held to 1e-12 relative."""
+the CSR and fused SELL variants re-associate and are held to 1e-12
+relative."""
 import numpy as np
 import pytest
 
@@ -19,7 +20,7 @@ def _lp(instances, m, n, k, seed=0):
 
 
 @pytest.mark.parametrize("shape", SHAPES)
-@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
 def test_multiply_matches_oracle(shape, variant, instances, oracle_lib):
     b = binding()
     L = b.lib()

@@ -39,6 +39,19 @@ sys.path.insert(0, ROOT)
 inst = importlib.import_module("acd-alm_gb300.instances")
 
 
+def replica_totals(dist, tot_dev: float, tot_wall: float, steps: int, device=None):
+    """Whole-job totals of N independent replicas (one LP per rank per step,
+    no data-path collective): the time is the slowest rank's, the LPs are
+    every rank's.  Returns (LPs, device seconds, wall seconds)."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return steps, tot_dev, tot_wall
+    import torch
+    t = torch.tensor([tot_dev, tot_wall], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    tot_dev, tot_wall = t.tolist()
+    return steps * dist.get_world_size(), tot_dev, tot_wall
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -479,12 +492,8 @@ def main():
     torch.cuda.synchronize()
     launches = L.acdalm_launch_count() - launches0
     clk = clocks.stop()
-    tot_dev, tot_wall = sum(dev_s), sum(wall_s)
-    if dist:
-        t = torch.tensor([tot_dev, tot_wall], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        tot_dev, tot_wall = t.tolist()
-    n_lp = args.steps * world
+    n_lp, tot_dev, tot_wall = replica_totals(dist, sum(dev_s), sum(wall_s), args.steps,
+                                             device="cuda")
     value = n_lp / tot_dev
     e2e = n_lp / tot_wall
     k = inst.rel_kkt(lp, x, lam)

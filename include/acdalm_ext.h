@@ -118,10 +118,11 @@ int acdalm_batch_free(acdalm_batch_t * b);
  * the cores) prepare each LP's layouts in arrival order; requests are
  * admitted, in arrival order, while their device footprint fits
  * device_budget bytes (0 = 80% of the free memory) and fewer than
- * max_inflight solves run (0 = 128).  Each admitted LP runs on one CTA of
- * its own launch and stream, beside the others; a finished solve is retired
- * and its memory returned.  The result of an LP does not depend on what
- * else runs (one CTA, deterministic reductions). */
+ * max_inflight solves run (0 = 128).  Each admitted LP runs in its own
+ * launch and stream, beside the others: on one CTA up to 150,000 nonzeros,
+ * on a thread-block cluster of 4, 8 or 16 CTAs above that; a finished solve
+ * is retired and its memory returned.  The result of an LP does not depend
+ * on what else runs (a fixed team, deterministic reductions). */
 typedef struct acdalm_server acdalm_server_t;
 acdalm_server_t * acdalm_server_create(size_t device_budget, int max_inflight,
                                        int precision, double kkt_tol,

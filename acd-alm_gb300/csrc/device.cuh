@@ -255,6 +255,7 @@ struct GridTeam {
         unsigned epoch;   // reductions passed (the same count in every CTA)
 
         static constexpr bool kShared = false;
+        static constexpr bool kStreamHint = false;  // see load_chunk
 
         __device__ int nthreads() const { return gridDim.x * blockDim.x; }
         __device__ int tid() const { return blockIdx.x * blockDim.x + threadIdx.x; }
@@ -413,6 +414,7 @@ struct BlockTeam {
         int * status;     // the LP's status word in global memory
 
         static constexpr bool kShared = true;
+        static constexpr bool kStreamHint = false;  // see load_chunk
 
         __device__ int nthreads() const { return blockDim.x; }
         __device__ int tid() const { return threadIdx.x; }
@@ -461,6 +463,7 @@ struct ClusterTeam {
         int parity;
 
         static constexpr bool kShared = false;
+        static constexpr bool kStreamHint = false;  // see load_chunk
 
         __device__ explicit ClusterTeam(int * st) : status(st), parity(0)
         {
@@ -590,6 +593,100 @@ struct Chunk {
         V a[VEC];
 };
 
+// An L2 policy that evicts the lines it tags first: a matrix streamed once
+// through a product far larger than L2 should not push out the gathered
+// vector, which every row reuses.
+__device__ __forceinline__ unsigned long long evict_first_policy()
+{
+        unsigned long long p;
+        asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+        return p;
+}
+
+__device__ __forceinline__ int ld_stream(const int32_t * p, unsigned long long pol)
+{
+        int r;
+        asm("ld.global.nc.L2::cache_hint.s32 %0, [%1], %2;" : "=r"(r) : "l"(p), "l"(pol));
+        return r;
+}
+__device__ __forceinline__ double ld_stream(const double * p, unsigned long long pol)
+{
+        double r;
+        asm("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(r) : "l"(p), "l"(pol));
+        return r;
+}
+__device__ __forceinline__ float ld_stream(const float * p, unsigned long long pol)
+{
+        float r;
+        asm("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(r) : "l"(p), "l"(pol));
+        return r;
+}
+__device__ __forceinline__ int4 ld_stream_v4(const int32_t * p, unsigned long long pol)
+{
+        int4 r;
+        asm("ld.global.nc.L2::cache_hint.v4.s32 {%0, %1, %2, %3}, [%4], %5;"
+            : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+            : "l"(p), "l"(pol));
+        return r;
+}
+__device__ __forceinline__ double2 ld_stream_v2(const double * p, unsigned long long pol)
+{
+        double2 r;
+        asm("ld.global.nc.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;"
+            : "=d"(r.x), "=d"(r.y)
+            : "l"(p), "l"(pol));
+        return r;
+}
+__device__ __forceinline__ float4 ld_stream_v4(const float * p, unsigned long long pol)
+{
+        float4 r;
+        asm("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+            : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
+            : "l"(p), "l"(pol));
+        return r;
+}
+
+// The matrix entries of one step, tagged evict-first in L2 when `pol` is
+// nonzero (a team that streams a matrix once, kStreamHint), plain
+// read-only loads otherwise (a solve's team keeps its matrix in L2 across
+// iterations).
+template <int VEC, class V>
+__device__ __forceinline__ Chunk<VEC, V> load_chunk_hinted(const int32_t * col, const V * val,
+                                                           int64_t at, unsigned long long pol)
+{
+        Chunk<VEC, V> q;
+        if constexpr (VEC == 1) {
+                q.c[0] = ld_stream(col + at, pol);
+                q.a[0] = ld_stream(val + at, pol);
+        } else {
+                static_assert(VEC == 4, "vector slices hold 4 entries per lane");
+                int4 c = ld_stream_v4(col + at, pol);
+                q.c[0] = c.x;
+                q.c[1] = c.y;
+                q.c[2] = c.z;
+                q.c[3] = c.w;
+                if constexpr (sizeof(V) == 8) {
+                        double2 a = ld_stream_v2(val + at, pol);
+                        double2 b = ld_stream_v2(val + at + 2, pol);
+                        q.a[0] = a.x;
+                        q.a[1] = a.y;
+                        q.a[2] = b.x;
+                        q.a[3] = b.y;
+                } else {
+                        float4 a = ld_stream_v4(val + at, pol);
+                        q.a[0] = a.x;
+                        q.a[1] = a.y;
+                        q.a[2] = a.z;
+                        q.a[3] = a.w;
+                }
+        }
+        return q;
+}
+
+template <int VEC, class Team, class V>
+__device__ __forceinline__ Chunk<VEC, V> team_chunk(const Team & tm, const int32_t * col,
+                                                    const V * val, int64_t at);
+
 template <int VEC, class V>
 __device__ __forceinline__ Chunk<VEC, V> load_chunk(const int32_t * col, const V * val,
                                                     int64_t at)
@@ -621,6 +718,18 @@ __device__ __forceinline__ Chunk<VEC, V> load_chunk(const int32_t * col, const V
                 }
         }
         return q;
+}
+
+// The step loads of a team: evict-first for teams that stream (kStreamHint,
+// with their policy in tm.policy).
+template <int VEC, class Team, class V>
+__device__ __forceinline__ Chunk<VEC, V> team_chunk(const Team & tm, const int32_t * col,
+                                                    const V * val, int64_t at)
+{
+        if constexpr (Team::kStreamHint)
+                return load_chunk_hinted<VEC>(col, val, at, tm.policy);
+        else
+                return load_chunk<VEC>(col, val, at);
 }
 
 // Visits slices so each warp of the team gets a balanced share: slices come
@@ -756,7 +865,7 @@ __device__ __forceinline__ T slice_row_sum(const Team & tm, const SellDev<V> & o
         T acc = 0;
         if constexpr (Exact) {
                 for (int t = 0; t < sl.steps; t++, at += 32 * VEC) {
-                        Chunk<VEC, V> q = load_chunk<VEC>(op.col, op.val, at);
+                        Chunk<VEC, V> q = team_chunk<VEC>(tm, op.col, op.val, at);
                         T p[VEC];
 #pragma unroll
                         for (int j = 0; j < VEC; j++)
@@ -768,8 +877,8 @@ __device__ __forceinline__ T slice_row_sum(const Team & tm, const SellDev<V> & o
                 T acc2 = 0;
                 int t = 0;
                 for (; t + 2 <= sl.steps; t += 2, at += 64 * VEC) {
-                        Chunk<VEC, V> q0 = load_chunk<VEC>(op.col, op.val, at);
-                        Chunk<VEC, V> q1 = load_chunk<VEC>(op.col, op.val, at + 32 * VEC);
+                        Chunk<VEC, V> q0 = team_chunk<VEC>(tm, op.col, op.val, at);
+                        Chunk<VEC, V> q1 = team_chunk<VEC>(tm, op.col, op.val, at + 32 * VEC);
                         T x0[VEC], x1[VEC];
 #pragma unroll
                         for (int j = 0; j < VEC; j++) {
@@ -783,7 +892,7 @@ __device__ __forceinline__ T slice_row_sum(const Team & tm, const SellDev<V> & o
                         }
                 }
                 if (t < sl.steps) {
-                        Chunk<VEC, V> q0 = load_chunk<VEC>(op.col, op.val, at);
+                        Chunk<VEC, V> q0 = team_chunk<VEC>(tm, op.col, op.val, at);
 #pragma unroll
                         for (int j = 0; j < VEC; j++)
                                 acc = madd<false>((T)q0.a[j], tm.ld(x + q0.c[j]), acc);
@@ -841,7 +950,7 @@ __device__ __forceinline__ void sell_rows_2p(const Team & tm, const SellDev<V> &
                         constexpr int VEC = decltype(w)::value;
                         int64_t at = sl.base + VEC * lane;
                         for (int t = 0; t < sl.steps; t++, at += 32 * VEC) {
-                                Chunk<VEC, V> q = load_chunk<VEC>(op.col, op.val, at);
+                                Chunk<VEC, V> q = team_chunk<VEC>(tm, op.col, op.val, at);
                                 T p[VEC], r[VEC];
 #pragma unroll
                                 for (int j = 0; j < VEC; j++) {

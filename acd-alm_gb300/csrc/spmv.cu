@@ -28,7 +28,11 @@
 namespace acd {
 
 // Grid-stride warps over a whole (non-cooperative) launch; x is read-only.
+// The matrix is streamed once per product, so its loads are tagged
+// evict-first in L2 and the gathered x keeps its lines.
 struct FlatTeam {
+        static constexpr bool kStreamHint = true;
+        unsigned long long policy = evict_first_policy();
         __device__ int nthreads() const { return gridDim.x * blockDim.x; }
         __device__ int tid() const { return blockIdx.x * blockDim.x + threadIdx.x; }
         __device__ int warp() const { return tid() >> 5; }

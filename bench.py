@@ -412,7 +412,12 @@ def main():
 
     if args.impl == "reference":
         if rank == 0:
-            run_reference(args, lp, rank)
+            if lp is None:
+                print(json.dumps({"impl": "reference",
+                                  "unavailable": "the CPU arm times single-LP workloads "
+                                                 "(mid, small, covering) only"}), flush=True)
+            else:
+                run_reference(args, lp, rank)
         return
 
     if args.spmv:

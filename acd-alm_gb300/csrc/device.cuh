@@ -224,6 +224,9 @@ struct TeamCtl {
 // Reduction slots: per CTA and parity one 128-byte line holding a 64-bit tag
 // (the barrier epoch that wrote it) and up to kRedMax values.
 constexpr int kSlotStride = 16;  // doubles per line
+// Lines a lane loads at once when it sums the CTAs' values: 12 covers 384
+// CTAs (2 per SM) in one round trip.
+constexpr int kSumWidth = 12;
 
 __device__ __forceinline__ void st_release_u64(unsigned long long * p, unsigned long long v)
 {
@@ -363,18 +366,18 @@ struct GridTeam {
                                 if (wk != k)
                                         continue;
                                 double idv = red_identity(op[k]);
-                                double vals[8];
+                                double vals[kSumWidth];
 #pragma unroll
-                                for (int q = 0; q < 8; q++) {
+                                for (int q = 0; q < kSumWidth; q++) {
                                         unsigned b = lane + 32u * q;
                                         vals[q] = (b < nb) ? __ldcg(lines + (size_t)b * kSlotStride + 1 + k)
                                                            : idv;
                                 }
                                 double acc = idv;
 #pragma unroll
-                                for (int q = 0; q < 8; q++)
+                                for (int q = 0; q < kSumWidth; q++)
                                         acc = red_combine(op[k], acc, vals[q]);
-                                for (unsigned b = lane + 256u; b < nb; b += 32)
+                                for (unsigned b = lane + 32u * kSumWidth; b < nb; b += 32)
                                         acc = red_combine(op[k], acc,
                                                           __ldcg(lines + (size_t)b * kSlotStride + 1 + k));
                                 acc = warp_reduce(acc, op[k]);

@@ -21,7 +21,7 @@ _u64p = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
 _sz = C.c_size_t
 _vp = C.c_void_p
 
-SPMV_SELL, SPMV_BLOCK, SPMV_CSR = 0, 1, 2
+SPMV_SELL, SPMV_BLOCK, SPMV_CSR, SPMV_SELL_FMA = 0, 1, 2, 3
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 
 ERRORS = {-1: "ACDALM_ECUDA", -2: "ACDALM_ETIMEOUT", -3: "ACDALM_ENOMEM",

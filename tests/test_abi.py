@@ -85,3 +85,38 @@ def test_bad_arguments_are_rejected(instances):
     with pytest.raises(b.AcdalmError):
         m.multiply(np.zeros(lp.ncols + 1))
     m.free()
+
+
+def test_spmv_variant_selector_range():
+    """acdalm_spmv_variant accepts the four variants and ignores anything
+    else, returning the previous selection (host-only, no GPU needed)."""
+    b = binding()
+    L = b.lib()
+    old = L.acdalm_spmv_variant(b.SPMV_SELL_FMA)
+    try:
+        assert L.acdalm_spmv_variant(b.SPMV_CSR) == b.SPMV_SELL_FMA
+        assert L.acdalm_spmv_variant(4) == b.SPMV_CSR
+        assert L.acdalm_spmv_variant(-1) == b.SPMV_CSR
+        assert L.acdalm_spmv_variant(b.SPMV_SELL) == b.SPMV_CSR
+    finally:
+        L.acdalm_spmv_variant(old)
+
+
+def test_sell_copy_rejects_short_buffers(instances):
+    """acdalm_sell_copy reports its sizes, then refuses buffers smaller
+    than those sizes instead of writing past them."""
+    b = binding()
+    L = b.lib()
+    lp = instances.small(seed=6, m=40, n=70, per_col=3)
+    m = b.Matrix(lp)
+    ns, ne = ctypes.c_size_t(), ctypes.c_size_t()
+    assert L.acdalm_sell_copy(m.h, 0, ctypes.byref(ns), ctypes.byref(ne),
+                              None, None, None, None, None) == 0
+    assert ns.value > 0 and ne.value >= lp.nnz and ne.value % 32 == 0
+    short = ctypes.c_size_t(ne.value - 1)
+    bufs = [np.zeros(ns.value + 1, np.int64), np.zeros(ns.value, np.int32),
+            np.zeros(ne.value, np.int32), np.zeros(ne.value), np.zeros(lp.nrows, np.int32)]
+    r = L.acdalm_sell_copy(m.h, 0, ctypes.byref(ns), ctypes.byref(short),
+                           *[x.ctypes.data_as(ctypes.c_void_p) for x in bufs])
+    assert r < 0
+    m.free()

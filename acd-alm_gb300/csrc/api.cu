@@ -277,6 +277,93 @@ alm_t * alm_read(FILE * stream)
                         llo.data(), lhi.data());
 }
 
+}  // extern "C"
+
+// ---- binary instances ----
+//
+// "ACDALMB1", then u64 nrows, ncols, nnz, then rows u32[nnz], columns
+// u32[nnz], values f64[nnz], rhs f64[nrows], linear, lower, upper f64[ncols],
+// dual lower, dual upper f64[nrows]; little-endian as the host writes it.
+// The same content as alm_read's text (alm.c:330-364), without parsing.
+
+namespace {
+
+const char kBinaryMagic[8] = {'A', 'C', 'D', 'A', 'L', 'M', 'B', '1'};
+
+template <class T>
+bool put(FILE * f, const T * p, size_t n)
+{
+        return n == 0 || fwrite(p, sizeof(T), n, f) == n;
+}
+
+template <class T>
+bool get(FILE * f, std::vector<T> & v, size_t n)
+{
+        v.resize(n);
+        return n == 0 || fread(v.data(), sizeof(T), n, f) == n;
+}
+
+}  // namespace
+
+extern "C" int acdalm_write_binary(alm_t * m, FILE * stream)
+{
+        if (!m || !stream) {
+                acd::set_error(ACDALM_EINVAL, "acdalm_write_binary: null argument");
+                return ACDALM_EINVAL;
+        }
+        sparse_matrix_t * a = alm_matrix(m);
+        size_t nrows = alm_nrhs(m), ncols = alm_nvars(m), nnz = sparse_matrix_nnz(a);
+        uint64_t hdr[3] = {nrows, ncols, nnz};
+        bool ok = put(stream, kBinaryMagic, 8) && put(stream, hdr, 3)
+                && put(stream, sparse_matrix_rows(a), nnz)
+                && put(stream, sparse_matrix_columns(a), nnz)
+                && put(stream, sparse_matrix_values(a), nnz)
+                && put(stream, alm_rhs(m), nrows) && put(stream, alm_linear(m), ncols)
+                && put(stream, alm_lower(m), ncols) && put(stream, alm_upper(m), ncols)
+                && put(stream, alm_lambda_lower(m), nrows)
+                && put(stream, alm_lambda_upper(m), nrows);
+        if (!ok) {
+                acd::set_error(ACDALM_EINVAL, "acdalm_write_binary: short write");
+                return ACDALM_EINVAL;
+        }
+        return 0;
+}
+
+extern "C" alm_t * acdalm_read_binary(FILE * stream)
+{
+        char magic[8];
+        uint64_t hdr[3];
+        if (!stream || fread(magic, 1, 8, stream) != 8 || memcmp(magic, kBinaryMagic, 8) != 0
+            || fread(hdr, sizeof(uint64_t), 3, stream) != 3) {
+                acd::set_error(ACDALM_EINVAL, "acdalm_read_binary: not an ACDALMB1 stream");
+                return nullptr;
+        }
+        uint64_t nrows = hdr[0], ncols = hdr[1], nnz = hdr[2];
+        if (nrows >= (1ull << 31) || ncols >= (1ull << 31) || nnz >= (1ull << 32)) {
+                acd::set_error(ACDALM_EINVAL, "acdalm_read_binary: sizes out of range");
+                return nullptr;
+        }
+        std::vector<uint32_t> rows, cols;
+        std::vector<double> vals, rhs, lin, lo, hi, llo, lhi;
+        if (!get(stream, rows, nnz) || !get(stream, cols, nnz) || !get(stream, vals, nnz)
+            || !get(stream, rhs, nrows) || !get(stream, lin, ncols) || !get(stream, lo, ncols)
+            || !get(stream, hi, ncols) || !get(stream, llo, nrows) || !get(stream, lhi, nrows)) {
+                acd::set_error(ACDALM_EINVAL, "acdalm_read_binary: truncated stream");
+                return nullptr;
+        }
+        sparse_matrix_t * mat = sparse_matrix_make(ncols, nrows, nnz, rows.data(), cols.data(),
+                                                   vals.data(), 0);
+        if (!mat)
+                return nullptr;
+        alm_t * m = alm_make(mat, nrows, rhs.data(), ncols, lin.data(), lo.data(), hi.data(),
+                             llo.data(), lhi.data());
+        if (!m)
+                sparse_matrix_free(mat);
+        return m;
+}
+
+extern "C" {
+
 // ---- extensions ----
 
 int alm_set_precision(struct alm * m, int mode)

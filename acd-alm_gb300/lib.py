@@ -82,6 +82,14 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.alm_make.restype = _vp
     L.alm_make.argtypes = [_vp, _sz, _f64p, _sz, _f64p, _vp, _vp, _vp, _vp]
     L.alm_free.argtypes = [_vp]
+    L.alm_matrix.restype = _vp
+    L.alm_matrix.argtypes = [_vp]
+    for f in ("nrhs", "nvars"):
+        getattr(L, "alm_" + f).restype = _sz
+        getattr(L, "alm_" + f).argtypes = [_vp]
+    L.acdalm_write_binary.argtypes = [_vp, _vp]
+    L.acdalm_read_binary.restype = _vp
+    L.acdalm_read_binary.argtypes = [_vp]
     L.alm_solve.argtypes = [_vp, _sz, _f64p, _sz, _f64p, _sz, _vp, _f64p, _vp]
     for f in ("rhs", "linear", "lower", "upper", "lambda_lower", "lambda_upper"):
         getattr(L, "alm_" + f).restype = C.POINTER(C.c_double)

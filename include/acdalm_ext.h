@@ -9,6 +9,7 @@
 #ifndef ACDALM_EXT_H
 #define ACDALM_EXT_H
 #include <stddef.h>
+#include <stdio.h>
 #include <stdint.h>
 #ifdef __cplusplus
 extern "C" {
@@ -191,6 +192,16 @@ struct sparse_matrix * acdalm_approx_permuted_matrix(struct approx * a);
  * (bit-identical to the reference's permuted instance). */
 int acdalm_approx_step_sizes(struct approx * a, double * beta, double * v,
                              double * inv_v);
+
+/* ---- binary instances ---- */
+/* The content of alm_read's text format (alm.h) in binary: the magic
+ * "ACDALMB1", u64 nrows, ncols, nnz, then the matrix's rows, columns (u32)
+ * and values (f64), rhs, linear, lower, upper, dual lower, dual upper
+ * (f64), host byte order.  No reference counterpart.  Write returns 0 or
+ * ACDALM_EINVAL; read returns a new instance owning a new matrix (free both
+ * as after alm_read) or NULL. */
+int acdalm_write_binary(struct alm * m, FILE * stream);
+struct alm * acdalm_read_binary(FILE * stream);
 
 /* ---- solving without allocating ---- */
 /* approx_solve for callers that cannot call cudaMalloc when they solve:

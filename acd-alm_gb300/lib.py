@@ -90,6 +90,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.acdalm_write_binary.argtypes = [_vp, _vp]
     L.acdalm_read_binary.restype = _vp
     L.acdalm_read_binary.argtypes = [_vp]
+    L.acdalm_read_mps.restype = _vp
+    L.acdalm_read_mps.argtypes = [_vp]
     L.alm_solve.argtypes = [_vp, _sz, _f64p, _sz, _f64p, _sz, _vp, _f64p, _vp]
     for f in ("rhs", "linear", "lower", "upper", "lambda_lower", "lambda_upper"):
         getattr(L, "alm_" + f).restype = C.POINTER(C.c_double)

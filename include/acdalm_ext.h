@@ -202,6 +202,14 @@ int acdalm_approx_step_sizes(struct approx * a, double * beta, double * v,
  * as after alm_read) or NULL. */
 int acdalm_write_binary(struct alm * m, FILE * stream);
 struct alm * acdalm_read_binary(FILE * stream);
+/* An LP in free-format MPS (ROWS, COLUMNS, RHS, RANGES, BOUNDS, OBJSENSE;
+ * integer markers ignored), as min c'x s.t. A x = b, l <= x <= u: every
+ * inequality or ranged row r gets a slack column (coefficient -1 in row r,
+ * bounded by the row's interval), appended after the file's columns in row
+ * order; equality rows stay equalities; multipliers are free; OBJSENSE MAX
+ * negates c.  Returns a new instance owning a new matrix, or NULL
+ * (acdalm_last_error names the line). */
+struct alm * acdalm_read_mps(FILE * stream);
 
 /* ---- solving without allocating ---- */
 /* approx_solve for callers that cannot call cudaMalloc when they solve:

@@ -132,3 +132,48 @@ def test_mps_errors_name_the_line(tmp_path):
     assert not _read(L, tmp_path, LP_MPS.replace("    RHS  C1  4.0", "    RHS  C9  4.0"),
                      "unknown.mps")
     assert b"unknown row" in L.acdalm_last_error()
+
+
+def _to_mps(lp):
+    """An equality-form LP (bounds finite, multipliers free) as free MPS."""
+    lines = ["NAME GEN", "ROWS", " N OBJ"]
+    lines += [f" E R{i}" for i in range(lp.nrows)]
+    lines.append("COLUMNS")
+    order = np.lexsort((lp.rows, lp.cols))
+    by_col = {}
+    for k in order:
+        by_col.setdefault(int(lp.cols[k]), []).append((int(lp.rows[k]), float(lp.vals[k])))
+    for j in range(lp.ncols):
+        lines.append(f"    C{j} OBJ {float(lp.linear[j])!r}")
+        for i, v in by_col.get(j, []):
+            lines.append(f"    C{j} R{i} {v!r}")
+    lines.append("RHS")
+    lines += [f"    RHS R{i} {float(lp.rhs[i])!r}" for i in range(lp.nrows)]
+    lines.append("BOUNDS")
+    for j in range(lp.ncols):
+        lines.append(f" LO BND C{j} {float(lp.lower[j])!r}")
+        lines.append(f" UP BND C{j} {float(lp.upper[j])!r}")
+    lines.append("ENDATA")
+    return "\n".join(lines) + "\n"
+
+
+def test_equality_lp_round_trips_through_mps(tmp_path, instances):
+    """An LP already in equality form comes back unchanged: no slack
+    columns, the same triplets and vectors, bit for bit (repr() of a double
+    parses back exactly)."""
+    b = binding()
+    L = b.lib()
+    lp = instances.small(seed=12, m=50, n=90, per_col=3)
+    h = _read(L, tmp_path, _to_mps(lp), "gen.mps")
+    assert h, L.acdalm_last_error()
+    m, n, (rows, cols, vals), vec = _instance(b, L, h)
+    assert (m, n) == (lp.nrows, lp.ncols)
+    got = sorted(zip(rows.tolist(), cols.tolist(), vals.tolist()))
+    want = sorted(zip(lp.rows.tolist(), lp.cols.tolist(), lp.vals.tolist()))
+    assert got == want
+    for k, v in (("rhs", lp.rhs), ("linear", lp.linear), ("lower", lp.lower),
+                 ("upper", lp.upper)):
+        assert vec[k].tobytes() == np.asarray(v, np.float64).tobytes(), k
+    mat = L.alm_matrix(h)
+    L.alm_free(h)
+    L.sparse_matrix_free(mat)

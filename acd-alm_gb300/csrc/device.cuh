@@ -7,11 +7,15 @@
 // rows over the team's warps, and team.reduce() is both the reduction and
 // the barrier between phases.
 //
-//   GridTeam  - every CTA of a cooperative launch (one large LP).  The
-//               barrier is a counter + generation word in global memory; the
-//               last CTA to arrive sums the per-CTA partials in CTA order and
-//               publishes the totals, so every CTA reads the same bits.
-//   BlockTeam - one CTA (one small LP of a batch); __syncthreads based.
+//   GridTeam    - every CTA of a cooperative launch (one large LP).  Each
+//                 CTA publishes its partials in its own line with a
+//                 release-stored epoch tag; every CTA waits for all tags and
+//                 sums all lines itself in CTA order, so every CTA reads the
+//                 same bits.
+//   BlockTeam   - one CTA (one small LP of a batch); __syncthreads based.
+//   ClusterTeam - the CTAs of one thread-block cluster (a large served LP);
+//                 partials read through distributed shared memory, hardware
+//                 cluster barriers.
 //
 // No wait is unbounded: a CTA that waits more than kWaitLimitNs for the
 // others records ACDALM_ETIMEOUT in the team's status word and every thread

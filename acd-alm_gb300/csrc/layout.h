@@ -8,10 +8,10 @@
 // and radix sorts instead of qsort); the outputs are the reference's.
 //
 // Part 2 builds the device layout the GPU kernels use: warp-sliced ELL
-// ("SELL-32") in a device order where rows are sorted by length, so a slice
-// of 32 rows has almost no padding.  Within a row, entries keep the
-// reference's order (ascending column of the permuted instance), so the
-// sequential per-row sums are the reference's sums.
+// ("SELL", one warp per slice) in a device order where rows are sorted by
+// length, so a slice's rows have almost no padding.  Within a row, entries
+// keep the reference's order (ascending column of the permuted instance),
+// so the sequential per-row sums are the reference's sums.
 #pragma once
 #include <cstddef>
 #include <cstdint>

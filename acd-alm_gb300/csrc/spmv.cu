@@ -2,7 +2,8 @@
 // layouts built by layout.cpp, with the products on the GPU.
 //
 // Three device variants of y = op(A) x:
-//   SELL  warp-sliced ELL over rows sorted by length (one lane per row);
+//   SELL  warp-sliced ELL over rows sorted by length (1 to 32 lanes per
+//         row, 1 or 4 entries per lane per step);
 //   BLOCK the reference's 4-row block arena, uploaded byte for byte, one
 //         quad of lanes per block (spmv_block.c:160-254);
 //   CSR   sub-warp per row over the reference's CSR arrays, shuffle sums.

@@ -35,7 +35,7 @@ unsigned long long acdalm_launch_count(void);
 int acdalm_take_error(void);
 
 /* ---- SpMV on the device ---- */
-#define ACDALM_SPMV_SELL 0  /* warp-sliced ELL, 32 rows per slice (default) */
+#define ACDALM_SPMV_SELL 0  /* warp-sliced ELL, one warp per slice (default) */
 #define ACDALM_SPMV_BLOCK 1 /* the 4-row block arena of the reference */
 #define ACDALM_SPMV_CSR 2   /* CSR, a sub-warp per row */
 /* SELL with fused multiply-adds and a lane tree per row: not bit-identical

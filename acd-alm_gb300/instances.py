@@ -63,6 +63,17 @@ class LP:
         return np.bincount(self.cols, weights=self.vals * y[self.rows],
                            minlength=self.ncols)
 
+    def sha256(self) -> str:
+        """SHA-256 over the arrays that define the LP, in a fixed order: a
+        fixture made from a seeded instance stores it, so a test can tell
+        that it rebuilt the same LP from the seed."""
+        import hashlib
+        h = hashlib.sha256()
+        for a in (self.rows, self.cols, self.vals, self.rhs, self.linear, self.lower,
+                  self.upper, self.lambda_lower, self.lambda_upper):
+            h.update(np.ascontiguousarray(a).tobytes())
+        return h.hexdigest()
+
 
 def _distinct_rows(rng: np.random.Generator, m: int, counts: np.ndarray):
     """For column j draw counts[j] distinct rows uniformly from [0, m).

@@ -120,6 +120,8 @@ class Lib:
                                         C.c_double, C.c_char_p, _sz, _f64p,
                                         C.c_double, C.c_int]
             L.ref_set_inner_budget.argtypes = [_sz]
+            L.ref_alm_solve_kkt.argtypes = [_vp, _sz, _f64p, _f64p, C.c_double, _f64p,
+                                            C.POINTER(_sz), C.c_int]
             L.ref_inner_used.restype = _sz
             L.ref_approx_internals.argtypes = [_vp, C.c_int, _u32p, _f64p, _f64p,
                                                _f64p, _f64p, _f64p, _f64p, _f64p]
@@ -273,3 +275,19 @@ class Lib:
             used = self.lib.ref_inner_used()
             self.lib.ref_set_inner_budget((1 << 64) - 1)
         return r, x, lam, diag, used
+
+    def alm_solve_kkt(self, h, nrows, ncols, tol, niter=1000, threads=1):
+        """The reference's alm_solve stopped at relative KKT <= tol (checked
+        at the start of every outer iteration after the first); reference
+        library only.  Returns (ret, x, lambda, [primal, dual, gap, c'x],
+        outer iterations, inner iterations)."""
+        assert self.kind == "ref"
+        x = np.zeros(ncols)
+        lam = np.zeros(nrows)
+        kk = np.zeros(4)
+        outer = _sz()
+        self.lib.ref_set_inner_budget((1 << 64) - 1)
+        r = self.lib.ref_alm_solve_kkt(h, niter, x, lam, tol, kk, C.byref(outer),
+                                       threads if threads > 1 else 0)
+        inner = self.lib.ref_inner_used()
+        return r, x, lam, kk, outer.value, inner

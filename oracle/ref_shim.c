@@ -22,6 +22,8 @@
  *     so they can be driven from Python through ctypes.
  */
 #include <assert.h>
+#include <math.h>
+#include <setjmp.h>
 #include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -36,6 +38,69 @@
 
 static size_t inner_budget = (size_t)-1;
 static size_t inner_used = 0;
+
+/* Optional relative-KKT stop (the metric's stop rule), armed by
+ * ref_alm_solve_kkt: at the entry of every inner solve after the first --
+ * i.e. at the start of outer iteration k > 0, where x is the previous inner
+ * solve's output and lambda has just been updated (alm.c:247-287) -- the
+ * residuals of (x, lambda) are computed with the reference's own SpMV:
+ *
+ *   primal = |A x - b|_2 / (1 + |b|_2)
+ *   dual   = |x - P[l,u](x - r)|_2 / (1 + |c|_2),  r = c - A' lambda
+ *            (the inner problem's linear term, approx_linear)
+ *   gap    = |c'x - (b'lambda + sum_j min(l_j r_j, u_j r_j))|
+ *            / (1 + |c'x| + |dual objective|)
+ *
+ * (b'lambda is the offset alm.c passes in).  When their maximum is at most
+ * the tolerance the solve is left by longjmp back into ref_alm_solve_kkt:
+ * x and lambda are the caller's arrays, so they hold exactly the point that
+ * was checked. */
+static struct {
+        int armed;
+        double tol;
+        const double * lambda;
+        const double * c0;
+        sparse_matrix_t * a;
+        size_t calls;
+        jmp_buf back;
+        double last[4];  /* primal, dual, gap, objective of the last check */
+} kkt;
+
+static void kkt_terms(const double * x, approx_t * approx, double offset,
+                      double out[4])
+{
+        size_t m = approx_nrhs(approx), n = approx_nvars(approx);
+        const double * b = approx_rhs(approx);
+        const double * r = approx_linear(approx);
+        const double * l = approx_lower(approx);
+        const double * u = approx_upper(approx);
+        double * ax = calloc(m ? m : 1, sizeof(double));
+        assert(0 == sparse_matrix_multiply(ax, m, kkt.a, x, n, 0, NULL));
+        double rr = 0, bb = 0;
+        for (size_t i = 0; i < m; i++) {
+                double d = ax[i] - b[i];
+                rr += d * d;
+                bb += b[i] * b[i];
+        }
+        free(ax);
+        double dd = 0, cc = 0, cx = 0, box = 0;
+        for (size_t j = 0; j < n; j++) {
+                double p = fmax(l[j], fmin(x[j] - r[j], u[j]));
+                double d = x[j] - p;
+                dd += d * d;
+                cc += kkt.c0[j] * kkt.c0[j];
+                cx += kkt.c0[j] * x[j];
+                double lo = isfinite(l[j]) ? l[j] * r[j] : HUGE_VAL;
+                double hi = isfinite(u[j]) ? u[j] * r[j] : HUGE_VAL;
+                double t = fmin(lo, hi);
+                box += isfinite(t) ? t : 0.0;
+        }
+        double dobj = offset + box;
+        out[0] = sqrt(rr) / (1 + sqrt(bb));
+        out[1] = sqrt(dd) / (1 + sqrt(cc));
+        out[2] = fabs(cx - dobj) / (1 + fabs(cx) + fabs(dobj));
+        out[3] = cx;
+}
 
 void ref_set_inner_budget(size_t budget)
 {
@@ -55,6 +120,12 @@ int cd_solve(double * x, size_t n, approx_t * approx, size_t niter,
 {
         double local[5];
         double * diag = (OUT_diagnosis != NULL) ? OUT_diagnosis : local;
+        if (kkt.armed && kkt.calls++ > 0) {
+                kkt_terms(x, approx, offset, kkt.last);
+                double rk = fmax(kkt.last[0], fmax(kkt.last[1], kkt.last[2]));
+                if (rk <= kkt.tol)
+                        longjmp(kkt.back, 1);
+        }
         if (inner_budget != (size_t)-1) {
                 size_t left = (inner_used < inner_budget)
                         ? inner_budget - inner_used : 0;
@@ -193,6 +264,42 @@ int ref_alm_solve(alm_t * alm, size_t niter, double * x, double * lambda,
         thread_pool_free(pool);
         if (log != NULL)
                 fclose(log);
+        return r;
+}
+
+/* alm_solve stopped at relative KKT <= tol, checked at the start of every
+ * outer iteration after the first (see cd_solve above).  Returns 0 when the
+ * tolerance was reached, else alm_solve's own return value; kkt_out (4
+ * doubles) receives primal, dual, gap and c'x of the last check, outer_out
+ * the outer iterations started.  On the stop the state alm_solve allocated
+ * for itself (one vector of nrhs doubles) is not freed: this is a fixture
+ * generator that runs once. */
+int ref_alm_solve_kkt(alm_t * alm, size_t niter, double * x, double * lambda,
+                      double tol, double * kkt_out, size_t * outer_out,
+                      int nthreads)
+{
+        thread_pool_t * pool = make_pool(nthreads);
+        kkt.armed = 1;
+        kkt.tol = tol;
+        kkt.lambda = lambda;
+        kkt.c0 = alm_linear(alm);
+        kkt.a = alm_matrix(alm);
+        kkt.calls = 0;
+        memset(kkt.last, 0, sizeof(kkt.last));
+        volatile int r;
+        volatile size_t outer;
+        if (setjmp(kkt.back) == 0) {
+                r = alm_solve(alm, niter, x, alm_nvars(alm), lambda,
+                              alm_nrhs(alm), NULL, NULL, pool);
+                outer = kkt.calls;
+        } else {
+                r = 0;
+                outer = kkt.calls - 1;  /* the check ran before this one */
+        }
+        kkt.armed = 0;
+        *outer_out = outer;
+        memcpy(kkt_out, kkt.last, sizeof(kkt.last));
+        thread_pool_free(pool);
         return r;
 }
 

@@ -120,3 +120,23 @@ def test_live_against_reference(shape, oracle_lib, ref_lib, instances):
     assert ro[0] == rr[0]
     assert ro[1].tobytes() == rr[1].tobytes()
     assert ro[2].tobytes() == rr[2].tobytes()
+
+
+def test_reference_kkt_stop_reproduces_small_fixture(ref_lib, instances):
+    """The reference's alm_solve stopped at relative KKT <= 1e-6
+    (ref_alm_solve_kkt, one thread) reproduces tests/golden/small_kkt.npz
+    bit for bit: the generator behind the KKT-stop fixtures is deterministic."""
+    g = np.load(os.path.join(GOLDEN, "small_kkt.npz"))
+    lp = instances.small()
+    assert lp.sha256() == str(g["instance_sha256"])
+    m = ref_lib.matrix(lp)
+    h = ref_lib.alm(m, lp)
+    r, x, lam, kk, outer, inner = ref_lib.alm_solve_kkt(h, lp.nrows, lp.ncols, 1e-6)
+    ref_lib.alm_free(h)
+    ref_lib.matrix_free(m)
+    assert r == int(g["ret"]) == 0
+    assert (outer, inner) == (int(g["outer"]), int(g["inner"]))
+    assert kk.tobytes() == g["kkt"].tobytes()
+    k = instances.rel_kkt(lp, x, lam)
+    assert k["rel_kkt"] <= 1e-6
+    assert k["objective"] == float(g["objective"])

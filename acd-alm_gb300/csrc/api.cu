@@ -52,6 +52,38 @@ int ensure_device(approx_t * a)
         return 0;
 }
 
+// The reference asserts that its iterates stay finite
+// (approx/step_project.inc:90, :577); a non-finite input makes them NaN
+// from the first step, so inputs are checked here instead: no NaN
+// anywhere, and infinities only in the bounds.
+int check_finite(const char * who, const char * what, const double * v, size_t n,
+                 bool bound)
+{
+        if (!v)
+                return 0;
+        for (size_t i = 0; i < n; i++) {
+                double e = v[i];
+                if (e != e || (!bound && std::isinf(e))) {
+                        acd::set_error(ACDALM_ENONFINITE, "%s: %s[%zu] is %g", who, what, i, e);
+                        return ACDALM_ENONFINITE;
+                }
+        }
+        return 0;
+}
+
+int check_approx_inputs(const char * who, approx_t * a, const double * x)
+{
+        int r;
+        if ((r = check_finite(who, "rhs", a->s_rhs.data(), a->nrhs, false))
+            || (r = check_finite(who, "weight", a->s_weight.data(), a->nrhs, false))
+            || (r = check_finite(who, "linear", a->s_linear.data(), a->nvars, false))
+            || (r = check_finite(who, "lower", a->s_lower.data(), a->nvars, true))
+            || (r = check_finite(who, "upper", a->s_upper.data(), a->nvars, true))
+            || (r = check_finite(who, "x", x, a->nvars, false)))
+                return r;
+        return 0;
+}
+
 acd::HostVectors shadow_vectors(approx_t * a)
 {
         acd::HostVectors hv;
@@ -139,8 +171,8 @@ int approx_solve(double * x, size_t n, approx_t * a, size_t niter, double max_pg
                 return ACDALM_EINVAL;
         }
         std::lock_guard<std::mutex> g(a->lock);
-        int r = ensure_device(a);
-        if (r)
+        int r = check_approx_inputs("approx_solve", a, x);
+        if (r || (r = ensure_device(a)))
                 return r;
         return acd::run_approx(a->dev, shadow_vectors(a), x, niter, max_pg, max_value,
                                min_delta, log, period, OUT_diagnosis, offset, a->stats);
@@ -157,8 +189,8 @@ int mpg_solve(double * x, size_t n, approx_t * a, size_t niter, double max_pg,
                 return ACDALM_EINVAL;
         }
         std::lock_guard<std::mutex> g(a->lock);
-        int r = ensure_device(a);
-        if (r)
+        int r = check_approx_inputs("mpg_solve", a, x);
+        if (r || (r = ensure_device(a)))
                 return r;
         return acd::run_mpg(a->dev, shadow_vectors(a), x, niter, max_pg, max_value, log,
                             period, OUT_diagnosis, offset, a->stats);
@@ -230,8 +262,20 @@ int alm_solve(alm_t * m, size_t niter, double * x, size_t nvars, double * lambda
         }
         approx_t * a = m->approx;
         std::lock_guard<std::mutex> g(a->lock);
-        int r = ensure_device(a);
-        if (r)
+        int r;
+        if ((r = check_finite("alm_solve", "rhs", a->rhs.data(), m->nrhs, false))
+            || (r = check_finite("alm_solve", "weight", a->weight.data(), m->nrhs, false))
+            || (r = check_finite("alm_solve", "linear", m->linear.data(), m->nvars, false))
+            || (r = check_finite("alm_solve", "lower", a->lower.data(), m->nvars, true))
+            || (r = check_finite("alm_solve", "upper", a->upper.data(), m->nvars, true))
+            || (r = check_finite("alm_solve", "lambda_lower", m->lambda_lower.data(), m->nrhs,
+                                 true))
+            || (r = check_finite("alm_solve", "lambda_upper", m->lambda_upper.data(), m->nrhs,
+                                 true))
+            || (r = check_finite("alm_solve", "x", x, m->nvars, false))
+            || (r = check_finite("alm_solve", "lambda", lambda, m->nrhs, false)))
+                return r;
+        if ((r = ensure_device(a)))
                 return r;
         // alm.c reads the live approx vectors each outer iteration
         acd::HostVectors hv;

@@ -32,6 +32,7 @@ constexpr int kRedMax = 8;                           // values per reduction
 constexpr unsigned long long kWaitLimitNs = 20ull * 1000000000ull;
 constexpr int kStatusTimeout = -2;                   // ACDALM_ETIMEOUT
 constexpr int kStatusNonFinite = -5;                 // ACDALM_ENONFINITE
+constexpr int kStatusTimeLimit = -7;                 // ACDALM_ETIMELIMIT
 
 enum RedOp { RED_SUM = 0, RED_MAX = 1, RED_MIN = 2 };
 

@@ -1,4 +1,5 @@
-// Solver kernels (one cooperative grid per LP) and their host launchers.
+// Host launchers of the solver kernels (kernels.cuh) and the small kernels
+// they need (permutation, step sizes).
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -10,13 +11,13 @@
 #include "common.h"
 #include "device.cuh"
 #include "instance.h"
+#include "kernels.cuh"
 #include "solver.cuh"
 
 namespace acd {
 
 namespace {
 
-constexpr int kThreads = 256;
 constexpr int kMaxTeamCtas = 1024;  // GridTeam's per-lane wait mask covers 32 x 32 CTAs
 constexpr int kLogCap = 1 << 14;
 
@@ -76,204 +77,6 @@ __global__ void step_size_kernel(SellDev<double> at, const double * w,
         }
 }
 
-struct AlmKernelArgs {
-        AlmProblem P;
-        AlmMixed M;
-        InnerWork<double> W;
-        LogBuf log;
-        AlmArgs a;
-        double * x;
-        double * lam;
-        TeamCtl * ctl;
-        double * slots;
-        double * result;
-        AlmOut * out;
-};
-
-template <bool Exact>
-__global__ void __launch_bounds__(kThreads, 2) alm_kernel(AlmKernelArgs k)
-{
-        GridTeam tm{k.ctl, k.slots, k.result, 0, 0u};
-        Alm<GridTeam, Exact> alm(tm, k.P, k.W, k.log, k.M);
-        AlmOut out;
-        memset(&out, 0, sizeof(out));
-        int r = alm.solve(k.a, k.x, k.lam, out);
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-                if (r < 0)
-                        out.ret = r;
-                *k.out = out;
-        }
-}
-
-struct ApproxOut {
-        int reason;
-        double diag[5];
-        long long iters;
-};
-
-struct ApproxKernelArgs {
-        InnerProblem<double> P;
-        InnerWork<double> W;
-        LogBuf log;
-        InnerArgs a;
-        double * x;
-        TeamCtl * ctl;
-        double * slots;
-        double * result;
-        ApproxOut * out;
-};
-
-template <bool Exact>
-__global__ void __launch_bounds__(kThreads, 2) approx_kernel(ApproxKernelArgs k)
-{
-        GridTeam tm{k.ctl, k.slots, k.result, 0, 0u};
-        Approx<double, GridTeam, Exact> ap(tm, k.P, k.W, k.log);
-        ApproxOut out;
-        memset(&out, 0, sizeof(out));
-        InnerArgs a = k.a;
-        a.t_start_ns = global_ns();
-        out.reason = ap.solve(a, k.x, out.diag, &out.iters);
-        if (blockIdx.x == 0 && threadIdx.x == 0)
-                *k.out = out;
-}
-
-// ---- spectral projected gradient (mpg_solve / spg_iter) ------------------
-//
-// approx.c:517-573 and mpg.inc:155-199.  The projection at the top of
-// spg_iter is skipped: x is always the output of a projection already
-// (the initial projection or the previous step), and clamping is
-// idempotent.
-template <class Team, bool Exact>
-struct Spg {
-        Approx<double, Team, Exact> & ap;
-        __device__ Spg(Approx<double, Team, Exact> & a) : ap(a) {}
-
-        __device__ int solve(const InnerArgs & a, double * x_io, double * diag,
-                             long long * iters_out)
-        {
-                auto & tm = ap.tm;
-                auto & P = ap.P;
-                auto & W = ap.W;
-                // state (approx.c:531-539): x = P(x0), z = x, g = grad(x), g2 = g
-                Vec<double> x = {W.xx, W.xv, 0, NAN, NAN};
-                double * z = W.zx;
-                double * g = W.g;
-                double * g2 = W.g2;
-                for (int j = tm.tid(); j < P.n; j += tm.nthreads()) {
-                        double xj = tm.ld(x_io + j);
-                        double lo = maxpd(tm.ld(P.l + j), xj);
-                        double v = minpd(lo, tm.ld(P.u + j));
-                        x.x[j] = v;
-                        z[j] = v;
-                }
-                if (!tm.sync())
-                        return -1;
-                double cx;
-                ap.x = x;
-                if (!ap.violation(ap.x, 0, 0, 0, true, false, &cx, nullptr, nullptr))
-                        return -1;
-                x = ap.x;
-                {
-                        double pg2, gg;
-                        if (!ap.gradient(x, false, pg2, gg))
-                                return -1;
-                }
-                for (int j = tm.tid(); j < P.n; j += tm.nthreads())
-                        g2[j] = tm.ld(g + j);
-                if (!tm.sync())
-                        return -1;
-                int reason = 0;
-                long long i;
-                for (i = 0; i < a.niter && !reason; i++) {
-                        // gradient at x, pg, y = x - z, u = g - g2, dots
-                        double part[4] = {0, 0, 0, 0};
-                        const int op[4] = {RED_SUM, RED_SUM, RED_SUM, RED_SUM};
-                        {
-                                sell_rows_1<Exact>(tm, P.At, x.viol, [&](int j, double s) {
-                                        double gj = s + tm.ld(P.c + j);
-                                        g[j] = gj;
-                                        double xj = tm.ld(x.x + j);
-                                        double xp = xj - gj;
-                                        xp = maxpd(tm.ld(P.l + j), xp);
-                                        xp = minpd(tm.ld(P.u + j), xp);
-                                        double d = xj - xp;
-                                        part[0] += d * d;
-                                        double yj = xj - tm.ld(z + j);
-                                        double uj = gj - tm.ld(g2 + j);
-                                        part[1] += yj * yj;
-                                        part[2] += yj * uj;
-                                });
-                        }
-                        if (!tm.reduce(part, op))
-                                return -1;
-                        double pg = sqrt(part[0]);
-                        double stepl = part[1] / part[2];
-                        if (stepl != stepl)
-                                stepl = 1;
-                        if (!(stepl > 1e8)) {
-                                // z = P(x - step g); swap(z, x); swap(g2, g)
-                                for (int j = tm.tid(); j < P.n; j += tm.nthreads()) {
-                                        double v = tm.ld(x.x + j) - stepl * tm.ld(g + j);
-                                        v = maxpd(tm.ld(P.l + j), v);
-                                        v = minpd(tm.ld(P.u + j), v);
-                                        z[j] = v;
-                                }
-                                if (!tm.sync())
-                                        return -1;
-                                double * t = z;
-                                z = x.x;
-                                x.x = t;
-                                t = g2;
-                                g2 = g;
-                                g = t;
-                                ap.W.g = g;
-                        }
-                        // value of the new x (its violation feeds the next
-                        // gradient)
-                        ap.x = x;
-                        if (!ap.violation(ap.x, 0, 0, 0, true, false, &cx, nullptr, nullptr))
-                                return -1;
-                        x = ap.x;
-                        double value = a.offset + x.quad + cx;
-                        if (pg < a.max_pg)
-                                reason = 2;
-                        if (value < a.max_value)
-                                reason = 1;
-                        if (a.log && ((a.period && (i % a.period == 0)) || i == 0 || reason)) {
-                                LogRec r = {2, 0, 0, 0, i + 1, {pg, value, 0, 0, 0, 0}};
-                                ap.put_log(r);
-                        }
-                }
-                // diagnosis (approx.c:556-569)
-                double pg2, gg;
-                if (!ap.gradient(x, false, pg2, gg))
-                        return -1;
-                for (int j = tm.tid(); j < P.n; j += tm.nthreads())
-                        x_io[j] = tm.ld(x.x + j);
-                if (!tm.sync())
-                        return -1;
-                diag[0] = a.offset + x.quad + cx;
-                diag[1] = sqrt(gg);
-                diag[2] = sqrt(pg2);
-                diag[3] = HUGE_VAL;
-                diag[4] = (double)(i + 1);
-                *iters_out = i;
-                (void)reason;
-                return 2;
-        }
-};
-
-__global__ void __launch_bounds__(kThreads, 2) mpg_kernel(ApproxKernelArgs k)
-{
-        GridTeam tm{k.ctl, k.slots, k.result, 0, 0u};
-        Approx<double, GridTeam, false> ap(tm, k.P, k.W, k.log);
-        Spg<GridTeam, false> spg(ap);
-        ApproxOut out;
-        memset(&out, 0, sizeof(out));
-        out.reason = spg.solve(k.a, k.x, out.diag, &out.iters);
-        if (blockIdx.x == 0 && threadIdx.x == 0)
-                *k.out = out;
-}
 
 // ---- host helpers --------------------------------------------------------
 
@@ -468,8 +271,22 @@ int read_status(DevInstance & d, int & status)
         return 0;
 }
 
+const char * status_text(int status)
+{
+        switch (status) {
+        case ACDALM_ETIMEOUT:
+                return "a device wait for the other CTAs of the team ran out";
+        case ACDALM_ETIMELIMIT:
+                return "the solve ran past its time limit, ACDALM_SOLVE_TIMEOUT";
+        case ACDALM_ENONFINITE:
+                return "an iterate stopped being finite";
+        default:
+                return "device failure";
+        }
+}
+
 // Whole-solve time limit on the device (ACDALM_SOLVE_TIMEOUT seconds,
-// default 900): a solve that runs longer stops with ACDALM_ETIMEOUT.
+// default 900): a solve that runs longer stops with ACDALM_ETIMELIMIT.
 unsigned long long solve_limit_ns()
 {
         const char * e = getenv("ACDALM_SOLVE_TIMEOUT");
@@ -479,11 +296,19 @@ unsigned long long solve_limit_ns()
         return (unsigned long long)(sec * 1e9);
 }
 
-int launch_coop(const void * fn, int max_blocks, void * args, cudaStream_t s)
+int launch_coop(const void * fn, int max_blocks, void * args, double * slots,
+                cudaStream_t s)
 {
         // every CTA must be resident at once: never more than the occupancy
         // of this kernel allows, nor more than the reduction slots hold
         int blocks = std::min(std::min(max_blocks, launch_blocks(fn)), kMaxTeamCtas);
+        // The grid team's reduction lines carry the epoch that wrote them,
+        // counted from 1 in every launch: a line left by an earlier launch
+        // on the same slots (one that ended after a few reductions, or
+        // failed) could carry a tag this launch waits for.  Zeroed lines
+        // never match.
+        ACD_CUDA_TRY(cudaMemsetAsync(slots, 0, 2 * (size_t)blocks * kSlotStride * sizeof(double),
+                                     s), ACDALM_ECUDA);
         void * params[1] = {args};
         ACD_CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kThreads),
                                                  params, 0, s), ACDALM_ECUDA);
@@ -504,10 +329,10 @@ int DevInstance::create(const DeviceLayout & lay)
         at_nslices = lay.at.nslices;
         max_width_a = lay.a.max_width;
         max_width_at = lay.at.max_width;
-        int blocks = std::max(std::max(launch_blocks((const void *)alm_kernel<false>),
-                                       launch_blocks((const void *)approx_kernel<false>)),
-                              std::max(launch_blocks((const void *)alm_kernel<true>),
-                                       launch_blocks((const void *)mpg_kernel)));
+        int blocks = std::max(std::max(launch_blocks(kernel_alm_grid(false)),
+                                       launch_blocks(kernel_approx_grid(false))),
+                              std::max(launch_blocks(kernel_alm_grid(true)),
+                                       launch_blocks(kernel_mpg_grid())));
         grid_blocks = blocks;
         size_t ea = lay.a.ptr.back(), eat = lay.at.ptr.back();
         size_t sa = std::max<size_t>(lay.a.row0.size(), 1), sat = std::max<size_t>(lay.at.row0.size(), 1);
@@ -815,9 +640,8 @@ static int alm_finish(DevInstance & d, const AlmKernelArgs & k, double * x, doub
         st.precision = k.a.mixed;
         st.inner_fp32 = out.inner32;
         if (status != 0) {
-                set_error(status, "device solve failed with status %d%s", status,
-                          status == ACDALM_ETIMEOUT ? " (a device wait timed out)"
-                          : status == ACDALM_ENONFINITE ? " (non-finite iterate)" : "");
+                set_error(status, "device solve failed with status %d (%s)", status,
+                          status_text(status));
                 return status;
         }
         if ((r = download_scatter(d, x, d.x, d.col_orig, d.n)) ||
@@ -847,9 +671,8 @@ int run_alm(DevInstance & d, const HostVectors & hv, size_t niter, double * x,
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
         cudaEventRecord(e0, d.stream);
-        const void * fn = g_exact ? (const void *)alm_kernel<true>
-                                  : (const void *)alm_kernel<false>;
-        if ((r = launch_coop(fn, d.grid_blocks, &k, d.stream)))
+        const void * fn = kernel_alm_grid(g_exact);
+        if ((r = launch_coop(fn, d.grid_blocks, &k, d.slots, d.stream)))
                 return r;
         cudaEventRecord(e1, d.stream);
         ACD_CUDA_TRY(cudaStreamSynchronize(d.stream), ACDALM_ECUDA);
@@ -862,82 +685,13 @@ int run_alm(DevInstance & d, const HostVectors & hv, size_t niter, double * x,
 
 // ---- batches: one LP per CTA ---------------------------------------------
 
-namespace {
-
-constexpr int kBatchThreads = 512;  // one LP per SM: 16 warps of memory parallelism
-
-// One LP on one CTA, its arguments passed by value (the server's launches).
-template <bool Exact>
-__global__ void __launch_bounds__(kBatchThreads, 1) alm_single_kernel(AlmKernelArgs k)
-{
-        BlockTeam tm{reinterpret_cast<int *>(&k.ctl->status_w.v)};
-        Alm<BlockTeam, Exact> alm(tm, k.P, k.W, k.log, k.M);
-        AlmOut out;
-        memset(&out, 0, sizeof(out));
-        int r = alm.solve(k.a, k.x, k.lam, out);
-        if (threadIdx.x == 0) {
-                if (r < 0)
-                        out.ret = r;
-                *k.out = out;
-        }
-}
-
-// Persistent CTAs take LPs from a shared counter (largest first) and run
-// each one's whole ALM solve with a one-CTA team.
-template <bool Exact>
-__global__ void __launch_bounds__(kBatchThreads, 1)
-alm_batch_kernel(const AlmKernelArgs * items, int count, int * next)
-{
-        __shared__ int cur;
-        for (;;) {
-                if (threadIdx.x == 0)
-                        cur = atomicAdd(next, 1);
-                __syncthreads();
-                int i = cur;
-                __syncthreads();
-                if (i >= count)
-                        break;
-                const AlmKernelArgs & k = items[i];
-                BlockTeam tm{reinterpret_cast<int *>(&k.ctl->status_w.v)};
-                Alm<BlockTeam, Exact> alm(tm, k.P, k.W, k.log, k.M);
-                AlmOut out;
-                memset(&out, 0, sizeof(out));
-                int r = alm.solve(k.a, k.x, k.lam, out);
-                if (threadIdx.x == 0) {
-                        if (r < 0)
-                                out.ret = r;
-                        *k.out = out;
-                }
-                __syncthreads();
-        }
-}
-
-}  // namespace
-
-// One LP on one thread-block cluster (launched with a cluster dimension).
-template <bool Exact>
-__global__ void __launch_bounds__(kBatchThreads, 1) alm_cluster_kernel(AlmKernelArgs k)
-{
-        ClusterTeam tm(reinterpret_cast<int *>(&k.ctl->status_w.v));
-        Alm<ClusterTeam, Exact> alm(tm, k.P, k.W, k.log, k.M);
-        AlmOut out;
-        memset(&out, 0, sizeof(out));
-        int r = alm.solve(k.a, k.x, k.lam, out);
-        if (tm.rank == 0 && threadIdx.x == 0) {
-                if (r < 0)
-                        out.ret = r;
-                *k.out = out;
-        }
-        // no CTA leaves while the others may still read its shared memory
-        tm.sync();
-}
 
 int max_cluster_team()
 {
         static int cached = 0;
         if (cached)
                 return cached;
-        const void * fn = (const void *)alm_cluster_kernel<false>;
+        const void * fn = kernel_alm_cluster(false);
         cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
         for (int q = 16; q >= 2; q /= 2) {
                 cudaLaunchConfig_t cfg = {};
@@ -989,13 +743,12 @@ int alm_launch_async(DevInstance & d, const HostVectors & hv, size_t niter, doub
                 ACD_CUDA_TRY(cudaEventCreateWithFlags(&h.done, cudaEventDisableTiming),
                              ACDALM_ECUDA);
         if (team == 1) {
-                if (g_exact)
-                        alm_single_kernel<true><<<1, kBatchThreads, 0, d.stream>>>(h.impl->k);
-                else
-                        alm_single_kernel<false><<<1, kBatchThreads, 0, d.stream>>>(h.impl->k);
+                void * params[1] = {&h.impl->k};
+                ACD_CUDA_TRY(cudaLaunchKernel(kernel_alm_single(g_exact), dim3(1),
+                                              dim3(kBatchThreads), params, 0, d.stream),
+                             ACDALM_ECUDA);
         } else {
-                const void * fn = g_exact ? (const void *)alm_cluster_kernel<true>
-                                          : (const void *)alm_cluster_kernel<false>;
+                const void * fn = kernel_alm_cluster(g_exact);
                 if (team > 8)
                         ACD_CUDA_TRY(cudaFuncSetAttribute(fn,
                                                           cudaFuncAttributeNonPortableClusterSizeAllowed,
@@ -1060,8 +813,7 @@ int run_alm_batch(std::vector<BatchEntry> & entries, size_t niter, double * seco
         ACD_CUDA_TRY(cudaMemcpyAsync(ditems, sorted.data(), sizeof(AlmKernelArgs) * count,
                                      cudaMemcpyHostToDevice, s), ACDALM_ECUDA);
         ACD_CUDA_TRY(cudaMemsetAsync(next, 0, sizeof(int), s), ACDALM_ECUDA);
-        const void * fn = g_exact ? (const void *)alm_batch_kernel<true>
-                                  : (const void *)alm_batch_kernel<false>;
+        const void * fn = kernel_alm_batch(g_exact);
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1071,10 +823,11 @@ int run_alm_batch(std::vector<BatchEntry> & entries, size_t niter, double * seco
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
         cudaEventRecord(e0, s);
-        if (g_exact)
-                alm_batch_kernel<true><<<blocks, kBatchThreads, 0, s>>>(ditems, count, next);
-        else
-                alm_batch_kernel<false><<<blocks, kBatchThreads, 0, s>>>(ditems, count, next);
+        {
+                void * params[3] = {&ditems, &count, &next};
+                ACD_CUDA_TRY(cudaLaunchKernel(fn, dim3(blocks), dim3(kBatchThreads), params, 0,
+                                              s), ACDALM_ECUDA);
+        }
         count_launch();
         ACD_CUDA_TRY(cudaGetLastError(), ACDALM_ECUDA);
         cudaEventRecord(e1, s);
@@ -1144,10 +897,8 @@ static int run_inner(DevInstance & d, const HostVectors & hv, double * x,
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
         cudaEventRecord(e0, d.stream);
-        const void * fn = mpg ? (const void *)mpg_kernel
-                        : (g_exact ? (const void *)approx_kernel<true>
-                                   : (const void *)approx_kernel<false>);
-        if ((r = launch_coop(fn, d.grid_blocks, &k, d.stream)))
+        const void * fn = mpg ? kernel_mpg_grid() : kernel_approx_grid(g_exact);
+        if ((r = launch_coop(fn, d.grid_blocks, &k, d.slots, d.stream)))
                 return r;
         cudaEventRecord(e1, d.stream);
         ACD_CUDA_TRY(cudaStreamSynchronize(d.stream), ACDALM_ECUDA);
@@ -1165,7 +916,8 @@ static int run_inner(DevInstance & d, const HostVectors & hv, double * x,
         st.inner = (unsigned long long)out.iters;
         st.status = status;
         if (status != 0) {
-                set_error(status, "device solve failed with status %d", status);
+                set_error(status, "device solve failed with status %d (%s)", status,
+                          status_text(status));
                 return status;
         }
         if ((r = download_scatter(d, x, d.x, d.col_orig, d.n)))
@@ -1259,9 +1011,8 @@ int run_approx_scratch(DevInstance & d, const HostVectors & hv, double * x_dev,
         k.slots = s.slots;
         k.result = s.result;
         k.out = static_cast<ApproxOut *>(s.out);
-        const void * fn = g_exact ? (const void *)approx_kernel<true>
-                                  : (const void *)approx_kernel<false>;
-        if ((r = launch_coop(fn, s.max_blocks, &k, stream)))
+        const void * fn = kernel_approx_grid(g_exact);
+        if ((r = launch_coop(fn, s.max_blocks, &k, s.slots, stream)))
                 return r;
         if (d.n) {
                 scatter_kernel<<<nb, 256, 0, stream>>>(x_dev, s.xd, d.col_orig, d.n);
@@ -1277,7 +1028,8 @@ int run_approx_scratch(DevInstance & d, const HostVectors & hv, double * x_dev,
                      ACDALM_ECUDA);
         ACD_CUDA_TRY(cudaStreamSynchronize(stream), ACDALM_ECUDA);
         if (status != 0) {
-                set_error(status, "device solve failed with status %d", status);
+                set_error(status, "device solve failed with status %d (%s)", status,
+                          status_text(status));
                 return status;
         }
         if (diag5)
@@ -1316,17 +1068,14 @@ void preload_solver_kernels()
         cudaFuncGetAttributes(&a, gather_kernel);
         cudaFuncGetAttributes(&a, scatter_kernel);
         cudaFuncGetAttributes(&a, step_size_kernel);
-        cudaFuncGetAttributes(&a, alm_kernel<false>);
-        cudaFuncGetAttributes(&a, alm_kernel<true>);
-        cudaFuncGetAttributes(&a, approx_kernel<false>);
-        cudaFuncGetAttributes(&a, approx_kernel<true>);
-        cudaFuncGetAttributes(&a, mpg_kernel);
-        cudaFuncGetAttributes(&a, alm_batch_kernel<false>);
-        cudaFuncGetAttributes(&a, alm_batch_kernel<true>);
-        cudaFuncGetAttributes(&a, alm_single_kernel<false>);
-        cudaFuncGetAttributes(&a, alm_single_kernel<true>);
-        cudaFuncGetAttributes(&a, alm_cluster_kernel<false>);
-        cudaFuncGetAttributes(&a, alm_cluster_kernel<true>);
+        for (int e = 0; e < 2; e++) {
+                cudaFuncGetAttributes(&a, kernel_alm_grid(e));
+                cudaFuncGetAttributes(&a, kernel_approx_grid(e));
+                cudaFuncGetAttributes(&a, kernel_alm_batch(e));
+                cudaFuncGetAttributes(&a, kernel_alm_single(e));
+                cudaFuncGetAttributes(&a, kernel_alm_cluster(e));
+        }
+        cudaFuncGetAttributes(&a, kernel_mpg_grid());
 }
 
 }  // namespace acd

@@ -60,7 +60,7 @@ struct InnerArgs {
         long long period;
         int log;         // record log lines
         unsigned long long t_start_ns;  // globaltimer at the solve's start
-        unsigned long long limit_ns;    // give up (ACDALM_ETIMEOUT) after this
+        unsigned long long limit_ns;    // give up (ACDALM_ETIMELIMIT) after this
         // When the iterate is a correction d to a point xbar (the mixed
         // precision mode), |xbar + d| is the norm the min_delta test uses.
         const double * xbar;
@@ -697,7 +697,7 @@ struct Approx {
                                 // bounded runtime: every thread sees the same
                                 // (reduced) elapsed time, so all stop together
                                 if (a.limit_ns && elapsed > (double)a.limit_ns) {
-                                        tm.fail(kStatusTimeout);
+                                        tm.fail(kStatusTimeLimit);
                                         return -1;
                                 }
                                 if (is_nan(x.value))

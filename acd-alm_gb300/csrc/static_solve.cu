@@ -2,12 +2,14 @@
 // device memory at solve time.
 //
 // Some callers of this library cannot call cudaMalloc when they solve:
-// code that runs while a CUDA stream is being captured into a graph (where
-// cudaMalloc is not allowed), frameworks whose caching allocator owns the
-// whole device memory budget, and latency-bound loops that cannot afford
-// cudaMalloc's implicit synchronisation.  This entry point uses no memory
-// beyond its inputs and outputs except one fixed array declared below, which
-// every GPU that loads the library holds until the process exits.
+// frameworks whose caching allocator has already taken the device memory
+// budget (a cudaMalloc beside it fails or fragments what it holds), and
+// latency-bound loops that cannot take cudaMalloc's implicit device-wide
+// synchronisation, which stalls every other stream.  This entry point uses
+// no memory beyond its inputs and outputs except one fixed array declared
+// below, which every GPU that loads the library holds until the process
+// exits.  Every call shares that array, so calls that overlap on the GPU
+// (from other threads or streams) race.
 #include <cuda_runtime.h>
 
 #include <mutex>

@@ -25,7 +25,8 @@ SPMV_SELL, SPMV_BLOCK, SPMV_CSR, SPMV_SELL_FMA = 0, 1, 2, 3
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 
 ERRORS = {-1: "ACDALM_ECUDA", -2: "ACDALM_ETIMEOUT", -3: "ACDALM_ENOMEM",
-          -4: "ACDALM_EINVAL", -5: "ACDALM_ENONFINITE", -6: "ACDALM_ENODEV"}
+          -4: "ACDALM_EINVAL", -5: "ACDALM_ENONFINITE", -6: "ACDALM_ENODEV",
+          -7: "ACDALM_ETIMELIMIT"}
 
 
 class Stats(C.Structure):

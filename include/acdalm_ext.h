@@ -22,6 +22,8 @@ extern "C" {
 #define ACDALM_EINVAL (-4)     /* bad argument (sizes, pointers, modes) */
 #define ACDALM_ENONFINITE (-5) /* the iterates stopped being finite */
 #define ACDALM_ENODEV (-6)     /* no usable CUDA device */
+#define ACDALM_ETIMELIMIT (-7) /* the solve ran past its time limit
+                                  (ACDALM_SOLVE_TIMEOUT seconds, default 900) */
 
 struct sparse_matrix;
 struct approx;
@@ -213,10 +215,9 @@ struct alm * acdalm_read_mps(FILE * stream);
 
 /* ---- solving without allocating ---- */
 /* approx_solve for callers that cannot call cudaMalloc when they solve:
- * code running while a CUDA stream is captured into a graph, frameworks
- * whose caching allocator owns the device memory budget, and latency-bound
- * loops that cannot take cudaMalloc's implicit synchronisation.  No
- * counterpart in the reference.
+ * frameworks whose caching allocator has already taken the device memory
+ * budget, and latency-bound loops that cannot take cudaMalloc's implicit
+ * device-wide synchronisation.  No counterpart in the reference.
  *
  * Same arguments and return values as approx_solve (approx.h), except: x is
  * a DEVICE array of n doubles (original order), updated in place; there is

@@ -77,3 +77,47 @@ def test_large_lp_runs_on_a_cluster(instances):
     k = instances.rel_kkt(lp, first[1], first[2])
     assert k["rel_kkt"] <= 1.01e-6, k
     assert first[1].tobytes() == again[1].tobytes()
+
+
+def _oracle_objective(oracle_lib, instances, lp, threads=1):
+    mo = oracle_lib.matrix(lp)
+    ho = oracle_lib.alm(mo, lp)
+    _, xo, lo, _, _ = oracle_lib.alm_solve(ho, lp.nrows, lp.ncols, threads=threads)
+    oracle_lib.alm_free(ho)
+    oracle_lib.matrix_free(mo)
+    return instances.rel_kkt(lp, xo, lo)["objective"]
+
+
+def test_served_lps_reach_oracle_optimum(instances, oracle_lib):
+    """Each LP served in a busy mix (mixed precision, the server's default)
+    reaches the optimum the oracle's own ALM solve finds, within what two
+    points that each meet a 1e-6 relative KKT tolerance can differ by."""
+    b = binding()
+    lps = _lps(instances, 8, 13)
+    res = _serve(b, lps, max_inflight=8)
+    for lp, (r, x, lam, st, lat) in zip(lps, res):
+        assert r == 0, st
+        k = instances.rel_kkt(lp, x, lam)
+        assert k["rel_kkt"] <= 1.01e-6, k
+        obj = _oracle_objective(oracle_lib, instances, lp)
+        assert abs(k["objective"] - obj) <= 1e-5 * (abs(obj) + 1), (k, obj)
+
+
+def test_large_lp_cluster_mixed_precision(instances, oracle_lib):
+    """The cluster team in the mixed form: FP32 inner iterations with the
+    float-float partials combined across the cluster's CTAs through
+    distributed shared memory, then the FP64 refinement.  It meets the FP64
+    stop, reaches the oracle's optimum and repeats bit for bit."""
+    b = binding()
+    lp = instances.batch_instance(12600, 78)  # 151,200 nonzeros: 4 CTAs
+    assert lp.nnz > 150000
+    first = _serve(b, [lp], max_inflight=4, precision=1)[0]
+    again = _serve(b, [lp, _lps(instances, 1, 98)[0]], max_inflight=4, precision=1)[0]
+    r, x, lam, st, _ = first
+    assert r == 0, st
+    assert st["precision"] == 1 and st["fp32_inner_iterations"] > 0, st
+    k = instances.rel_kkt(lp, x, lam)
+    assert k["rel_kkt"] <= 1.01e-6, k
+    assert x.tobytes() == again[1].tobytes()
+    obj = _oracle_objective(oracle_lib, instances, lp, threads=8)
+    assert abs(k["objective"] - obj) <= 1e-5 * (abs(obj) + 1), (k, obj)

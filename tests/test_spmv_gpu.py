@@ -116,3 +116,73 @@ def test_sell_slice_kinds_match_oracle(mode, instances, oracle_lib, monkeypatch)
         L.acdalm_spmv_variant(old)
     oracle_lib.matrix_free(mo)
     m.free()
+
+
+def test_fp32_long_rows_error_bound(instances):
+    """FP32 row sums on rows of 0..700 entries (every lane count).  The SELL
+    layout never gives one lane a chain of more than 64 products (rows over
+    16 entries spread over 4, 16 or 32 lanes, 4 entries per lane and step in
+    vector slices), and rows wider than 256 entries combine their lanes'
+    partial sums in FP64, so the accumulation error of a row stays within
+
+        |y32_i - y_i| <= (min(len_i, 64) + 4) * 2^-24 * sum_k |a_ik x_k|
+
+    against the exact product of the same FP32-rounded values and vector,
+    where one FP32 chain over a 700-entry row could be off by 704 units.
+    The CSR kernel is held to the plain (len_i + 4) bound.  Both are also
+    within 4 * 2^-24 * sum |a x| of that bound from the FP64 product of the
+    unrounded data."""
+    import torch
+    b = binding()
+    L = b.lib()
+    lp = ragged_lp(instances, 24)
+    m = b.Matrix(lp)
+    rng = np.random.default_rng(6)
+    u32 = 2.0 ** -24
+    lens = np.bincount(lp.rows, minlength=lp.nrows)
+    assert lens.max() > 600
+    x = rng.uniform(-1, 1, lp.ncols)
+    x32 = x.astype(np.float32)
+    a32 = lp.vals.astype(np.float32).astype(np.float64)
+    exact = np.bincount(lp.rows, weights=a32 * x32.astype(np.float64)[lp.cols],
+                        minlength=lp.nrows)
+    mag = np.bincount(lp.rows, weights=np.abs(a32 * x32.astype(np.float64)[lp.cols]),
+                      minlength=lp.nrows)
+    for variant, chain in ((0, np.minimum(lens, 64)), (2, lens)):
+        bound = (chain + 4) * u32 * mag
+        xd = torch.tensor(x32, device="cuda")
+        yd = torch.zeros(lp.nrows, dtype=torch.float32, device="cuda")
+        s = torch.cuda.current_stream().cuda_stream
+        assert L.acdalm_spmv_device_f32(m.h, variant, 0, xd.data_ptr(), yd.data_ptr(), s) == 0
+        torch.cuda.synchronize()
+        got = yd.double().cpu().numpy()
+        err = np.abs(got - exact)
+        assert (err <= bound).all(), (variant, np.max(err / np.maximum(bound, 1e-300)))
+        full = lp.matvec(x)
+        assert (np.abs(got - full) <= bound + 4 * u32 * mag).all(), variant
+    m.free()
+
+
+def test_mixed_solve_on_long_rows_reaches_oracle_optimum(instances, oracle_lib):
+    """The mixed-precision solve (FP32 inner iterations) on an LP whose rows
+    have up to 700 entries meets the FP64 stop and the oracle's optimum."""
+    b = binding()
+    lp = ragged_lp(instances, 25)
+    m = b.Matrix(lp)
+    alm = b.Alm(m, lp)
+    alm.set_kkt_tolerance(1e-6)
+    alm.set_precision(1)
+    r, x, lam, _ = alm.solve(1000)
+    st = alm.stats()
+    assert r == 0 and st["fp32_inner_iterations"] > 0, st
+    k = instances.rel_kkt(lp, x, lam)
+    assert k["rel_kkt"] <= 1.01e-6, k
+    mo = oracle_lib.matrix(lp)
+    ho = oracle_lib.alm(mo, lp)
+    _, xo, lo, _, _ = oracle_lib.alm_solve(ho, lp.nrows, lp.ncols)
+    ko = instances.rel_kkt(lp, xo, lo)
+    assert abs(k["objective"] - ko["objective"]) <= 1e-5 * (abs(ko["objective"]) + 1), (k, ko)
+    oracle_lib.alm_free(ho)
+    oracle_lib.matrix_free(mo)
+    alm.free()
+    m.free()

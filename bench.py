@@ -6,6 +6,9 @@ Workload (default): the mid-size LP, m=100,000 rows, n=200,000 columns,
 Zipf(1.5) column counts (~2.26M nonzeros), values U[-1,1], box [0,10],
 seeded synthetic data.
 
+The headline form is the plain FP64 solve (the drop-in for the reference's
+FP64 alm_solve); the FP32 + FP64-refinement form is reported beside it.
+
 Printed (rank 0, one JSON line):
   value         LPs/s from the solve kernel's device time (inputs resident in
                 HBM; L2 flushed with a 512 MB write before every step)
@@ -15,6 +18,8 @@ Printed (rank 0, one JSON line):
                 measured HBM copy bandwidth
   cpu_baseline  the reference's CPU loop on this host's cores, on a bounded
                 sample of the same workload (see `sample`)
+  mixed_form    the same LP in the mixed form: LPs/s, iterations, and its
+                objective's distance from the FP64 form's and the reference's
 
   python bench.py [--steps K] [--warmup W] [--precision fp64|mixed]
                   [--workload mid|small] [--impl reference]
@@ -302,12 +307,31 @@ class ClockSampler:
                 "samples": len(rows), "reasons": sorted(reasons)}
 
 
-def cpu_baseline(lp, gpu_inner_per_lp: float, iters: int, threads: int):
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def reference_solve_record(workload: str):
+    """The reference's own solve of this workload to relative KKT <= 1e-6
+    (inner iterations, objective), recorded by running the reference
+    compiled from its sources (tests/golden/make_kkt_golden.py): the
+    iterations a CPU solve of this LP takes.  None if not recorded."""
+    name = {"mid": "mid.npz", "small": "small_kkt.npz"}.get(workload)
+    path = os.path.join(GOLDEN, name) if name else None
+    if not path or not os.path.exists(path):
+        return None
+    g = np.load(path)
+    return {"inner_iterations": int(g["inner"]), "outer_iterations": int(g["outer"]),
+            "objective": float(g["objective"]), "rel_kkt": float(g["host_kkt"][3]),
+            "source": f"tests/golden/{name}"}
+
+
+def cpu_baseline(lp, inner_per_lp: float, iters: int, threads: int, per_lp_source: str):
     """The reference's inner loop on the host cores, over a bounded sample:
     `iters` APPROX iterations on the same LP (the loop that dominates a
     solve: ~23 outer vs ~10^5 inner iterations), one ALM outer iteration's
-    set-up included; LPs/s is extrapolated with the GPU solve's inner
-    iterations per LP."""
+    set-up included; LPs/s is projected with `inner_per_lp` inner
+    iterations per LP (the reference's own count for this LP where it was
+    recorded)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     kind = "reference" if O.available("ref") else "port"
@@ -327,36 +351,58 @@ def cpu_baseline(lp, gpu_inner_per_lp: float, iters: int, threads: int):
     done = int(diag[4]) if diag[4] > 0 else iters
     iters = min(iters, done)
     per_iter = dt / max(iters, 1)
-    return {"value": 1.0 / (per_iter * gpu_inner_per_lp), "unit": "LP/s",
+    return {"value": 1.0 / (per_iter * inner_per_lp), "unit": "LP/s",
             "cores": threads, "kind": kind,
             "sample": (f"{iters} APPROX iterations of the same LP on {threads} threads "
-                       f"({dt:.1f} s, {per_iter * 1e3:.2f} ms/iteration), extrapolated to "
-                       f"{gpu_inner_per_lp:.0f} inner iterations per LP (the FP64 GPU solve's "
-                       f"count for the same LP; the outer ALM work is <1% of a solve)")}
+                       f"({dt:.1f} s, {per_iter * 1e3:.3f} ms/iteration), projected to "
+                       f"{inner_per_lp:.0f} inner iterations per LP ({per_lp_source}; the "
+                       f"outer ALM work is <1% of a solve)"),
+            "sample_seconds": dt, "sample_iterations": iters,
+            "ms_per_iteration": per_iter * 1e3, "inner_iterations_per_lp": inner_per_lp}
+
+
+def inner_per_lp_of(args, fallback=None):
+    """Inner iterations per LP for the CPU projection: the reference's own
+    count for this workload where recorded, else `fallback` (the GPU FP64
+    solve's count), else a round figure.  Returns (count, source)."""
+    rec = reference_solve_record(args.workload)
+    if rec:
+        return float(rec["inner_iterations"]), (
+            f"the reference's own count for this LP, {rec['source']}")
+    if fallback:
+        return float(fallback), "the FP64 GPU solve's count for the same LP"
+    return 100000.0, "a round figure: no recorded count for this workload"
 
 
 def run_reference(args, lp, rank: int):
     """--impl reference: the reference's CPU implementation of the loop on
     the host cores (oracle/_ref where it was compiled, else the oracle port),
-    each step a bounded sample of the workload."""
+    each step a bounded sample of the workload: --ref-iters APPROX
+    iterations.  ms_per_step is that sample's time; value (LPs/s) projects
+    the sample's time per iteration to the reference's own iterations per
+    LP, and the projection's terms are in `projection`."""
     threads = os.cpu_count() or 1
-    # inner iterations per LP of this workload, as the GPU solve measured
-    per_lp = float(os.environ.get("ACDALM_REF_ITERS_PER_LP",
-                                  {"mid": "116480", "small": "14690"}.get(args.workload,
-                                                                          "100000")))
-    vals = []
+    per_lp, source = inner_per_lp_of(args)
+    vals, secs = [], []
     base = None
     for s in range(args.warmup + args.steps):
-        base = cpu_baseline(lp, per_lp, args.ref_iters, threads)
+        base = cpu_baseline(lp, per_lp, args.ref_iters, threads, source)
         if s >= args.warmup:
             vals.append(base["value"])
+            secs.append(base["sample_seconds"])
     v = statistics.median(vals)
     base["value"] = v
+    cfg = config_of(args, lp)
+    cfg["precision"] = "fp64"
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "LP/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": config_of(args, lp), "cpu_baseline": base,
+            "ms_per_step": 1e3 * statistics.mean(secs), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": cfg, "cpu_baseline": base,
+            "projection": {"ms_per_iteration": base["ms_per_iteration"],
+                           "inner_iterations_per_lp": per_lp, "source": source,
+                           "seconds_per_lp": 1.0 / v,
+                           "step": f"{args.ref_iters} APPROX iterations (a bounded sample)"},
             "e2e": {"value": v, "unit": "LP/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     if rank == 0:
@@ -365,12 +411,15 @@ def run_reference(args, lp, rank: int):
 
 METRIC = "LPs/sec to 1e-6 relative KKT"
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one FP32 inner
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one FP64 inner
 # iteration of the mid LP's solve kernel, from one ncu capture of
-# `bench.py --profile-solve 3000` (3,000 FP32 iterations; see
-# profiles/alm_kernel_mid_traffic.md).  FP64 iterations are scaled by their
+# `bench.py --profile-solve 3000 --precision fp64` (3,000 FP64 iterations;
+# profiles/alm_kernel_mid_traffic.md).  FP32 iterations are scaled by their
 # algorithmic bytes.
-MID_DRAM_BYTES_PER_FP32_ITER = (7724266240 + 3569961216) / 3000
+MID_DRAM_BYTES_PER_FP64_ITER = (7724266240 + 3569961216) / 3000 * 85470432.0 / 52380288.0
+TRAFFIC_NOTE = ("ncu DRAM bytes per launch, scaled from a 3,000-iteration capture of the "
+                "same kernel; the instance stays in L2, so traffic is far below the "
+                "algorithmic bytes")
 
 
 def config_of(args, lp):
@@ -387,14 +436,17 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--workload", default="mid")
-    ap.add_argument("--precision", default="mixed")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
+                    help="the headline form (fp64: the reference's arithmetic)")
     ap.add_argument("--profile-solve", type=int, default=0,
                     help="run one ALM solve capped at this many inner iterations and exit "
                          "(the command the ncu captures use)")
-    ap.add_argument("--ref-iters", type=int, default=8000,
-                    help="APPROX iterations each CPU sample times (about 10 s on 16 cores)")
+    ap.add_argument("--ref-iters", type=int, default=4000,
+                    help="APPROX iterations each CPU sample times (about 6 s on 16 cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-fp64-side", action="store_true")
+    ap.add_argument("--side-steps", type=int, default=2,
+                    help="solves of the other precision form, reported beside the "
+                         "headline (0 = none)")
     ap.add_argument("--spmv", action="store_true",
                     help="time the device SpMV variants on the workload's matrix")
     ap.add_argument("--spmv-reps", type=int, default=10)
@@ -503,16 +555,27 @@ def main():
     e2e = n_lp / tot_wall
     k = inst.rel_kkt(lp, x, lam)
     fp32 = args.precision == "mixed"
-    fp64_side = None
-    if fp32 and not args.no_fp64_side:
-        # the plain FP64 form of the same solve, for comparison
-        alm.set_precision(lib.PRECISION_FP64)
-        r64, x64, l64, st64, wall64 = one_step()
-        fp64_side = {"value": 1.0 / st64["seconds"], "unit": "LP/s",
-                     "inner_iterations": st64["inner_iterations"],
-                     "rel_kkt": st64["rel_kkt"],
-                     "objective": inst.rel_kkt(lp, x64, l64)["objective"]}
-        alm.set_precision(lib.PRECISION_MIXED)
+    ref_rec = reference_solve_record(args.workload)
+    side = None
+    if args.side_steps > 0:
+        # the other precision form of the same solve, for comparison
+        other = "fp64" if fp32 else "mixed"
+        alm.set_precision(lib.PRECISION_FP64 if fp32 else lib.PRECISION_MIXED)
+        sides = [one_step() for _ in range(args.side_steps)]
+        alm.set_precision(lib.PRECISION_MIXED if fp32 else lib.PRECISION_FP64)
+        r2, x2, l2, st2, _ = sides[-1]
+        k2 = inst.rel_kkt(lp, x2, l2)
+        sec2 = statistics.median(s_[3]["seconds"] for s_ in sides)
+        side = {"precision": other, "value": 1.0 / sec2, "unit": "LP/s",
+                "device_seconds": [s_[3]["seconds"] for s_ in sides],
+                "inner_iterations": st2["inner_iterations"],
+                "fp32_inner_iterations": st2["fp32_inner_iterations"],
+                "rel_kkt_host_check": k2["rel_kkt"], "objective": k2["objective"],
+                "objective_rel_diff_vs_headline":
+                    abs(k2["objective"] - k["objective"]) / abs(k["objective"])}
+        if ref_rec:
+            side["objective_rel_diff_vs_reference"] = (
+                abs(k2["objective"] - ref_rec["objective"]) / abs(ref_rec["objective"]))
     bpi = bytes_per_iteration(lp, False)
     bpi32 = bytes_per_iteration(lp, True)
     mean_inner = float(np.mean(inner))
@@ -522,9 +585,9 @@ def main():
     achieved = algo_bytes / (tot_dev / args.steps) / 1e9
     peak, peak_kind = load_peaks()
     traffic = None
-    if args.workload == "mid" and fp32:
-        traffic = MID_DRAM_BYTES_PER_FP32_ITER * (
-            mean_inner32 + (mean_inner - mean_inner32) * bpi / bpi32)
+    if args.workload == "mid":
+        traffic = (MID_DRAM_BYTES_PER_FP64_ITER * (mean_inner - mean_inner32)
+                   + MID_DRAM_BYTES_PER_FP64_ITER * bpi32 / bpi * mean_inner32)
     line = {
         "metric": METRIC, "value": value, "unit": "LP/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
@@ -537,26 +600,27 @@ def main():
                 "d2h_bytes_per_step": 8 * (2 * lp.ncols + 2 * lp.nrows)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                     "traffic_note": "ncu DRAM bytes per launch, scaled from a 3,000-iteration "
-                                     "capture; the instance stays in L2, so traffic is far "
-                                     "below the algorithmic bytes",
+                     "traffic_note": TRAFFIC_NOTE,
                      "kernel": "alm_kernel (persistent cooperative solve)",
                      "peak_source": peak_kind,
                      "bytes_per_inner_iteration": {"fp64": bpi, "fp32": bpi32}},
         "gpu_launches": int(launches),
-        "fp64_form": fp64_side,
+        ("fp64_form" if fp32 else "mixed_form"): side,
         "solve": {"inner_iterations": inner, "fp32_inner_iterations": inner32,
                   "outer_iterations": outer,
                   "rel_kkt_device": kkts, "rel_kkt_host_check": k["rel_kkt"],
                   "objective": k["objective"], "device_seconds": dev_s,
                   "wall_seconds": wall_s},
+        "reference_solve": ref_rec,
         "clocks": clk,
     }
+    if ref_rec:
+        line["solve"]["objective_rel_diff_vs_reference"] = (
+            abs(k["objective"] - ref_rec["objective"]) / abs(ref_rec["objective"]))
     if rank == 0 and not args.no_cpu_baseline:
-        # the CPU loop runs in FP64: extrapolate with the FP64 solve's count
-        per_lp = fp64_side["inner_iterations"] if fp64_side else mean_inner
+        per_lp, source = inner_per_lp_of(args, fallback=mean_inner if not fp32 else None)
         line["cpu_baseline"] = cpu_baseline(lp, per_lp, args.ref_iters,
-                                            os.cpu_count() or 1)
+                                            os.cpu_count() or 1, source)
     if rank == 0:
         print(json.dumps(line), flush=True)
     alm.free()

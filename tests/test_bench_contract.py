@@ -34,3 +34,27 @@ def test_fp32_iteration_moves_fewer_bytes():
     for m, n, nnz in ((1, 1, 1), (1000, 2000, 10_000), (10 ** 6, 5 * 10 ** 6, 33 * 10 ** 6)):
         lp = _Shape(m, n, nnz)
         assert b.bytes_per_iteration(lp, True) < b.bytes_per_iteration(lp, False)
+
+
+def test_reference_arm_line_fits_its_own_run(monkeypatch, capsys, instances):
+    """--impl reference: each step is a bounded sample, ms_per_step is that
+    sample's measured time (so steps x ms_per_step is the run's length), the
+    LPs/s value is a projection whose terms are reported, the precision is
+    FP64, and the iterations per LP are the reference's own recorded count."""
+    import json
+    import sys
+    b = _bench()
+    monkeypatch.setattr(b, "workload", lambda name: instances.small())
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--workload", "small",
+                                      "--steps", "2", "--warmup", "1", "--ref-iters", "300"])
+    b.main()
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["dtype"] == "f64"
+    assert line["config"]["precision"] == "fp64"
+    p = line["projection"]
+    assert p["inner_iterations_per_lp"] == 14500  # tests/golden/small_kkt.npz
+    assert "small_kkt.npz" in p["source"]
+    assert line["ms_per_step"] < 60_000
+    assert abs(line["value"] * p["ms_per_iteration"] * 1e-3 * p["inner_iterations_per_lp"]
+               - 1.0) < 0.5
+    assert line["e2e"]["value"] == line["value"]

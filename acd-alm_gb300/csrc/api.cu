@@ -40,7 +40,7 @@ int ensure_device(approx_t * a)
         if (!acd::device_ready())
                 return ACDALM_ENODEV;
         if (!a->lay_ready) {
-                acd::build_device_layout(acd::host_of(a->permuted), a->lay);
+                acd::build_device_layout(acd::host_of(a->permuted), a->lay, a->lay_max_steps);
                 a->lay_ready = true;
         }
         int r = a->dev.create(a->lay);
@@ -502,6 +502,14 @@ acdalm_batch_t * acdalm_batch_make(struct alm * const * instances, size_t count)
         if (!b)
                 return nullptr;
         b->alms.assign(instances, instances + count);
+        // one CTA per LP: device layouts not built yet are built for it
+        // (full lanes, no step cap); instances already solved keep theirs
+        for (size_t i = 0; i < count; i++) {
+                approx_t * a = instances[i]->approx;
+                std::lock_guard<std::mutex> g(a->lock);
+                if (!a->lay_ready)
+                        a->lay_max_steps = 0;
+        }
         return b;
 }
 
@@ -565,6 +573,37 @@ int acdalm_batch_solve(acdalm_batch_t * b, size_t niter, double * const * x,
 double acdalm_batch_seconds(acdalm_batch_t * b)
 {
         return b ? b->seconds : 0;
+}
+
+int alm_set_trace(struct alm * m, uint64_t first, uint64_t count)
+{
+        if (!m || first > 0xffffffffull || count > (1u << 20)) {
+                acd::set_error(ACDALM_EINVAL, "alm_set_trace: reductions %llu + %llu",
+                               (unsigned long long)first, (unsigned long long)count);
+                return ACDALM_EINVAL;
+        }
+        m->settings.trace_first = (unsigned)first;
+        m->settings.trace_count = (unsigned)count;
+        return 0;
+}
+
+int alm_trace_copy(struct alm * m, uint64_t * out, size_t cap, size_t * ctas, size_t * count)
+{
+        if (!m) {
+                acd::set_error(ACDALM_EINVAL, "alm_trace_copy: NULL instance");
+                return ACDALM_EINVAL;
+        }
+        approx_t * a = m->approx;
+        std::lock_guard<std::mutex> g(a->lock);
+        if (!a->dev_ready) {
+                if (ctas)
+                        *ctas = 0;
+                if (count)
+                        *count = 0;
+                return 0;
+        }
+        return acd::copy_trace(a->dev, reinterpret_cast<unsigned long long *>(out), cap, ctas,
+                               count);
 }
 
 // Step sizes as the solver computes them, in original order: beta (m), v,

@@ -5,9 +5,20 @@
 #include <cstdint>
 #include <string>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/acdalm_ext.h"
 
 namespace acd {
+
+// A named host-side range for NVTX-aware profilers (upload, solve kernel,
+// download, ...); costs nothing when no profiler is attached.
+struct NvtxRange {
+        explicit NvtxRange(const char * name) { nvtxRangePushA(name); }
+        ~NvtxRange() { nvtxRangePop(); }
+        NvtxRange(const NvtxRange &) = delete;
+        NvtxRange & operator=(const NvtxRange &) = delete;
+};
 
 // Records the last error of the calling thread (read back through
 // acdalm_last_error) and, unless ACDALM_QUIET is set, prints it to stderr.

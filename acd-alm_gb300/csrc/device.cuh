@@ -187,6 +187,49 @@ __device__ __forceinline__ P warp_reduce(P v, int op)
         return v;
 }
 
+__device__ __forceinline__ double shfl_xor(double v, int o)
+{
+        return __shfl_xor_sync(0xffffffffu, v, o);
+}
+__device__ __forceinline__ DF shfl_xor(DF v, int o)
+{
+        return {__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+}
+
+// Warp reduction of KP = 1, 2, 4 or 8 values at once (a transposing
+// butterfly): at offsets 16, 8, ... each lane keeps half of its slots --
+// the upper half if its lane bit is set -- and adds its partner's copy of
+// them, so each level costs KP/2 additions instead of KP; after log2 KP
+// levels every lane holds one slot, and a plain tree over the remaining
+// 32/KP lanes finishes it.  Slot k's total ends in lane k * (32/KP).  For
+// KP = 8 that is 9 additions per lane where 8 separate trees take 40: on
+// this GPU's narrow FP64 pipe, most of the cost of a block reduction.  The
+// order of the additions is fixed, so the result is deterministic.
+template <int KP, class P>
+__device__ __forceinline__ P warp_reduce_many(P (&v)[KP], int (&op)[KP], int lane)
+{
+#pragma unroll
+        for (int h = KP / 2, off = 16; h >= 1; h /= 2, off /= 2) {
+                bool hi = (lane & off) != 0;
+#pragma unroll
+                for (int j = 0; j < h; j++) {
+                        P keep = hi ? v[h + j] : v[j];
+                        P give = hi ? v[j] : v[h + j];
+                        int o = hi ? op[h + j] : op[j];
+                        P got = shfl_xor(give, off);
+                        // the lower lane's value first, in both lanes' view
+                        v[j] = hi ? red_combine(o, got, keep) : red_combine(o, keep, got);
+                        op[j] = o;
+                }
+        }
+        P r = v[0];
+        int o = op[0];
+#pragma unroll
+        for (int off = 16 / KP; off > 0; off >>= 1)
+                r = red_combine(o, r, shfl_down(r, off));
+        return r;
+}
+
 // Block-wide reduction of K partials (double or DF); the totals, as
 // doubles, land in out[0..K) (shared) and are visible to every thread of
 // the block on return.
@@ -194,24 +237,33 @@ template <int K, class P>
 __device__ __forceinline__ void block_reduce(const P (&v)[K], const int (&op)[K],
                                              double * out)
 {
+        constexpr int KP = K <= 1 ? 1 : K <= 2 ? 2 : K <= 4 ? 4 : 8;
+        constexpr int G = 32 / KP;
+        static_assert(K <= kRedMax, "at most kRedMax values per reduction");
         __shared__ P part[kWarp][kRedMax];
         int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         int nw = (blockDim.x + 31) >> 5;
+        P w[KP];
+        int o[KP];
 #pragma unroll
-        for (int k = 0; k < K; k++) {
-                P r = warp_reduce(v[k], op[k]);
-                if (lane == 0)
-                        part[warp][k] = r;
+        for (int k = 0; k < KP; k++) {
+                o[k] = k < K ? op[k] : RED_SUM;
+                w[k] = k < K ? v[k] : red_identity_as<P>(RED_SUM);
         }
+        P r = warp_reduce_many<KP>(w, o, lane);
+        if ((lane & (G - 1)) == 0 && lane / G < K)
+                part[warp][lane / G] = r;
         __syncthreads();
         if (warp == 0) {
+                // the warps' totals, lane q holding warp q's: the same butterfly
 #pragma unroll
-                for (int k = 0; k < K; k++) {
-                        P r = (lane < nw) ? part[lane][k] : red_identity_as<P>(op[k]);
-                        r = warp_reduce(r, op[k]);
-                        if (lane == 0)
-                                out[k] = to_double(r);
+                for (int k = 0; k < KP; k++) {
+                        o[k] = k < K ? op[k] : RED_SUM;
+                        w[k] = (k < K && lane < nw) ? part[lane][k] : red_identity_as<P>(o[k]);
                 }
+                P t = warp_reduce_many<KP>(w, o, lane);
+                if ((lane & (G - 1)) == 0 && lane / G < K)
+                        out[lane / G] = to_double(t);
         }
         __syncthreads();
 }
@@ -232,22 +284,20 @@ constexpr int kSlotStride = 16;  // doubles per line
 // Lines a lane loads at once when it sums the CTAs' values: 12 covers 384
 // CTAs (2 per SM) in one round trip.
 constexpr int kSumWidth = 12;
-
-__device__ __forceinline__ void st_release_u64(unsigned long long * p, unsigned long long v)
-{
-        asm volatile("st.release.gpu.global.u64 [%0], %1;" :: "l"(p), "l"(v) : "memory");
-}
-
 __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long * p)
 {
         unsigned long long v;
         asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
         return v;
 }
-
 __device__ __forceinline__ void fence_acquire_gpu()
 {
         asm volatile("fence.acq_rel.gpu;" ::: "memory");
+}
+
+__device__ __forceinline__ void st_release_u64(unsigned long long * p, unsigned long long v)
+{
+        asm volatile("st.release.gpu.global.u64 [%0], %1;" :: "l"(p), "l"(v) : "memory");
 }
 
 // Every CTA of a cooperative launch.  team.reduce() is an all-gather: each
@@ -255,12 +305,35 @@ __device__ __forceinline__ void fence_acquire_gpu()
 // every CTA waits for all tags of this epoch and sums all lines itself in
 // CTA order -- so every thread gets the same bits, in about two L2 round
 // trips, with no counters and no fences.
+// Phase timestamps of the grid team's reductions (optional): for the
+// reductions first .. first + count - 1 (counted from 1 in each launch), CTA
+// b's thread 0 records %globaltimer at kTracePhases points -- entering the
+// reduction (its warp 0's share of the pass done), after the block
+// reduction (the whole CTA done), and leaving it (every CTA's partials
+// summed) -- at rec[((e - first) * gridDim.x + b) * kTracePhases + phase].
+constexpr int kTracePhases = 3;
+struct TraceBuf {
+        unsigned long long * rec;  // nullptr: tracing off
+        unsigned first, count;
+};
+
 struct GridTeam {
         TeamCtl * ctl;
         double * slots;   // [2][gridDim.x][kSlotStride]
         double * result;  // unused (kept for the launch interface)
         int parity;
         unsigned epoch;   // reductions passed (the same count in every CTA)
+        TraceBuf trace;
+
+        __device__ void stamp(unsigned e, int phase) const
+        {
+                if (trace.rec && threadIdx.x == 0) {
+                        unsigned i = e - trace.first;
+                        if (e >= trace.first && i < trace.count)
+                                trace.rec[((size_t)i * gridDim.x + blockIdx.x) * kTracePhases
+                                          + phase] = global_ns();
+                }
+        }
 
         static constexpr bool kShared = false;
         static constexpr bool kStreamHint = false;  // see load_chunk
@@ -296,8 +369,10 @@ struct GridTeam {
         {
                 __shared__ double tot[kRedMax];
                 __shared__ int bad;
+                stamp(epoch + 1, 0);
                 block_reduce<K>(v, op, tot);
                 epoch++;
+                stamp(epoch, 1);
                 const unsigned nb = gridDim.x;
                 double * lines = slots + (size_t)parity * nb * kSlotStride;
                 if (threadIdx.x == 0) {
@@ -393,6 +468,7 @@ struct GridTeam {
                 if (threadIdx.x == 0)
                         bad = status_now != 0;
                 __syncthreads();
+                stamp(epoch, 2);
 #pragma unroll
                 for (int k = 0; k < K; k++)
                         res[k] = tot[k];

@@ -55,6 +55,10 @@ struct DevInstance {
         int log_cap = 0;
         void * out = nullptr;          // AlmOut / approx output block
         int grid_blocks = 0;           // cooperative grid size
+        // phase timestamps of the last traced grid solve (alm_set_trace)
+        unsigned long long * trace_rec = nullptr;
+        size_t trace_cap = 0;          // records the buffer holds
+        size_t trace_ctas = 0, trace_count = 0;  // of the last traced launch
         int block_threads = 256;
 
         // FP32 copies for the mixed precision mode (allocated on first use)
@@ -89,6 +93,8 @@ struct AlmSettings {
         unsigned long long inner_budget = 0;
         double kkt_tol = 0;
         int precision = 0;
+        // grid-team reductions first .. first + count - 1 are traced
+        unsigned trace_first = 0, trace_count = 0;
 };
 
 struct SolveStats {
@@ -128,6 +134,12 @@ struct BatchEntry {
 // first.  Returns 0 or the first negative code; each entry's ret holds its
 // own outcome.  *seconds receives the device time of the launch.
 int run_alm_batch(std::vector<BatchEntry> & entries, size_t niter, double * seconds);
+
+// The phase timestamps of the instance's last traced grid solve
+// (AlmSettings::trace_*): ctas x count x kTracePhases values, or only the
+// sizes when out is null.
+int copy_trace(DevInstance & d, unsigned long long * out, size_t cap, size_t * ctas,
+               size_t * count);
 
 // One asynchronous ALM solve on one CTA (the server's unit of work): the
 // launch records `done` on the instance's stream.

@@ -311,7 +311,7 @@ int vector_mode()
 // decreasing length); its entries keep their CSR order, columns mapped
 // through col_map (identity if empty).
 void build_sell(Sell & s, const Csr & c, const std::vector<int32_t> & src_of_d,
-                const std::vector<int32_t> & col_map)
+                const std::vector<int32_t> & col_map, int max_steps)
 {
         int n = (int)src_of_d.size();
         int mode = vector_mode();
@@ -329,6 +329,15 @@ void build_sell(Sell & s, const Csr & c, const std::vector<int32_t> & src_of_d,
         for (int d = 0; d < n;) {
                 uint32_t first = len_of(d);
                 int L1 = lanes_for(first), L4 = lanes_for(cdiv(first, kVec));
+                if (max_steps > 0) {
+                        // more lanes per row until the slice takes at most
+                        // max_steps steps (rows are in decreasing length, so
+                        // the first row is the slice's longest)
+                        while (L1 < kSlice && cdiv(first, L1) > (uint32_t)max_steps)
+                                L1 *= 2;
+                        while (L4 < kSlice && cdiv(first, kVec * L4) > (uint32_t)max_steps)
+                                L4 *= 2;
+                }
                 uint32_t cap1 = cdiv(first, L1) * L1, cap4 = cdiv(first, kVec * L4) * kVec * L4;
                 bool vec = mode == 1 || (mode == 2 && 8 * (uint64_t)cap4 <= 9 * (uint64_t)cap1);
                 int L = vec ? L4 : L1, V = vec ? kVec : 1;
@@ -396,7 +405,13 @@ void build_sell(Sell & s, const Csr & c, const std::vector<int32_t> & src_of_d,
 
 }  // namespace
 
-void build_device_layout(const HostMatrix & pm, DeviceLayout & out)
+int grid_max_steps()
+{
+        const char * e = getenv("ACDALM_SELL_STEPS");
+        return e ? atoi(e) : 8;
+}
+
+void build_device_layout(const HostMatrix & pm, DeviceLayout & out, int max_steps)
 {
         int m = (int)pm.nrows, n = (int)pm.ncols;
         out.m = m;
@@ -420,15 +435,16 @@ void build_device_layout(const HostMatrix & pm, DeviceLayout & out)
                 out.col_d_of_p[p] = d;
                 out.col_orig_of_d[d] = (int32_t)pm.cperm.idx[p];
         }
-        build_sell(out.a, pm.csr, out.row_p_of_d, out.col_d_of_p);
-        build_sell(out.at, pm.csr_t, out.col_p_of_d, out.row_d_of_p);
+        out.max_steps = max_steps;
+        build_sell(out.a, pm.csr, out.row_p_of_d, out.col_d_of_p, max_steps);
+        build_sell(out.at, pm.csr_t, out.col_p_of_d, out.row_d_of_p, max_steps);
 }
 
 void build_plain_sell(const HostMatrix & m, bool transpose, PlainSell & out)
 {
         const Csr & c = transpose ? m.csr_t : m.csr;
         out.row_of_d = order_by_length(c.ptr);
-        build_sell(out.s, c, out.row_of_d, {});
+        build_sell(out.s, c, out.row_of_d, {}, 0);
 }
 
 }  // namespace acd

@@ -58,8 +58,8 @@ void ensure_zorder(HostMatrix & m);
 
 // Warp-sliced ELL of one operator (A or A') in device order, with a
 // per-slice height and lane width.  A slice is 32 lanes wide and holds
-// h = 32 / L consecutive rows, each row spread over L lanes (L = 1, 4, 16 or
-// 32, chosen from the slice's longest row).  A slice is either scalar (a
+// h = 32 / L consecutive rows, each row spread over L lanes (L a power of
+// two up to 32, chosen from the slice's longest row).  A slice is either scalar (a
 // lane holds V = 1 entry of its row per step) or vector (V = 4 consecutive
 // entries per step, so one 16-byte load fetches 4 column indices and one or
 // two 16-byte loads their values).  Entry k of the slice's r-th row sits at
@@ -86,13 +86,24 @@ struct DeviceLayout {
         std::vector<int32_t> row_p_of_d, row_d_of_p, row_orig_of_d;
         std::vector<int32_t> col_p_of_d, col_d_of_p, col_orig_of_d;
         std::vector<double> beta;  // nonzeros per device row
+        int max_steps = 0;         // the step cap the slices were built with
         Sell a, at;
 };
 
 // `pm` is the permuted copy (approx.c:84-88); its CSR orders fix the
 // summation order.  Device rows (columns) are the permuted instance's rows
 // (columns) sorted by decreasing length, ties by position.
-void build_device_layout(const HostMatrix & pm, DeviceLayout & out);
+//
+// max_steps > 0 spreads the rows of a slice over more lanes (up to 32) until
+// the slice takes at most max_steps steps: a team solving one LP on the
+// whole GPU waits for its slowest warp every pass, and a warp's time is its
+// chain of dependent steps.  0 keeps the width rule alone (teams of one CTA
+// or one cluster, which are throughput bound and prefer full lanes).
+void build_device_layout(const HostMatrix & pm, DeviceLayout & out, int max_steps);
+
+// The max_steps of layouts for whole-GPU solves (alm_solve, approx_solve,
+// mpg_solve): ACDALM_SELL_STEPS, else 8.
+int grid_max_steps();
 
 // SELL of a plain matrix (no permutation involved), for the SpMV API:
 // device order = rows sorted by length; transpose selects A'.

@@ -19,6 +19,9 @@ struct approx {
         std::vector<double> s_rhs, s_weight, s_linear, s_lower, s_upper;
         acd::DeviceLayout lay;
         bool lay_ready = false;
+        // the step cap of the device layout built on first use: whole-GPU
+        // solves by default; batches build theirs for one-CTA teams (0)
+        int lay_max_steps = acd::grid_max_steps();
         acd::DevInstance dev;
         bool dev_ready = false;
         acd::SolveStats stats;

@@ -110,7 +110,7 @@ void build_one(acdalm_server_t * s, Request * r)
                                   r->lhi.data());
         if (r->alm) {
                 approx_t * a = r->alm->approx;
-                acd::build_device_layout(acd::host_of(a->permuted), a->lay);
+                acd::build_device_layout(acd::host_of(a->permuted), a->lay, 0);
                 a->lay_ready = true;
                 r->team = std::min(team_size((long long)r->vals.size()), s->max_team);
                 // the COO copies are not needed any more

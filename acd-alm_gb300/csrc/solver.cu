@@ -297,7 +297,7 @@ unsigned long long solve_limit_ns()
 }
 
 int launch_coop(const void * fn, int max_blocks, void * args, double * slots,
-                cudaStream_t s)
+                cudaStream_t s, int * launched = nullptr)
 {
         // every CTA must be resident at once: never more than the occupancy
         // of this kernel allows, nor more than the reduction slots hold
@@ -313,6 +313,8 @@ int launch_coop(const void * fn, int max_blocks, void * args, double * slots,
         ACD_CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kThreads),
                                                  params, 0, s), ACDALM_ECUDA);
         count_launch();
+        if (launched)
+                *launched = blocks;
         return 0;
 }
 
@@ -480,6 +482,10 @@ int DevInstance::ensure_f32(const DeviceLayout & lay)
 
 void DevInstance::destroy()
 {
+        if (trace_rec)
+                cudaFreeAsync(trace_rec, stream);
+        trace_rec = nullptr;
+        trace_cap = trace_ctas = trace_count = 0;
         if (mem32)
                 cudaFreeAsync(mem32, stream);
         mem32 = nullptr;
@@ -617,6 +623,56 @@ static int alm_prepare(DevInstance & d, const HostVectors & hv, size_t niter, do
         return 0;
 }
 
+// The trace buffer of a grid solve when the settings ask for one: grown on
+// the instance's stream as needed and zeroed; trace.rec stays null otherwise.
+static int prepare_trace(DevInstance & d, const AlmSettings & s, TraceBuf & trace)
+{
+        trace = {nullptr, 0, 0};
+        if (s.trace_count == 0)
+                return 0;
+        size_t need = (size_t)s.trace_count * d.grid_blocks * kTracePhases;
+        if (d.trace_cap < need) {
+                if (d.trace_rec)
+                        cudaFreeAsync(d.trace_rec, d.stream);
+                d.trace_rec = nullptr;
+                d.trace_cap = 0;
+                void * p = nullptr;
+                cudaError_t e = cudaMallocAsync(&p, need * sizeof(unsigned long long), d.stream);
+                if (e != cudaSuccess) {
+                        set_error(ACDALM_ENOMEM, "trace buffer (%zu bytes): %s",
+                                  need * sizeof(unsigned long long), cudaGetErrorString(e));
+                        return ACDALM_ENOMEM;
+                }
+                d.trace_rec = static_cast<unsigned long long *>(p);
+                d.trace_cap = need;
+        }
+        ACD_CUDA_TRY(cudaMemsetAsync(d.trace_rec, 0, need * sizeof(unsigned long long), d.stream),
+                     ACDALM_ECUDA);
+        trace = {d.trace_rec, s.trace_first, s.trace_count};
+        return 0;
+}
+
+// Copies the last traced launch's records (see TraceBuf).
+int copy_trace(DevInstance & d, unsigned long long * out, size_t cap, size_t * ctas,
+               size_t * count)
+{
+        if (ctas)
+                *ctas = d.trace_ctas;
+        if (count)
+                *count = d.trace_count;
+        size_t n = d.trace_ctas * d.trace_count * kTracePhases;
+        if (!out || n == 0)
+                return 0;
+        if (cap < n) {
+                set_error(ACDALM_EINVAL, "alm_trace_copy: %zu records need %zu values, buffer "
+                          "holds %zu", d.trace_count, n, cap);
+                return ACDALM_EINVAL;
+        }
+        ACD_CUDA_TRY(cudaMemcpy(out, d.trace_rec, n * sizeof(unsigned long long),
+                                cudaMemcpyDeviceToHost), ACDALM_ECUDA);
+        return 0;
+}
+
 // Reads one instance's outcome after its ALM kernel finished.
 static int alm_finish(DevInstance & d, const AlmKernelArgs & k, double * x, double * lam,
                       FILE * log, double * diag3, double * w_out, double * c_out,
@@ -663,23 +719,38 @@ int run_alm(DevInstance & d, const HostVectors & hv, size_t niter, double * x,
             double * lam, FILE * log, double * diag3, const AlmSettings & s,
             double * w_out, double * c_out, SolveStats & st, const DeviceLayout * lay)
 {
+        NvtxRange solve_range("acdalm alm_solve");
         AlmKernelArgs k;
-        int r = alm_prepare(d, hv, niter, x, lam, log != nullptr, s, lay, k);
-        if (r)
-                return r;
+        int r;
+        {
+                NvtxRange up("acdalm upload");
+                if ((r = alm_prepare(d, hv, niter, x, lam, log != nullptr, s, lay, k)))
+                        return r;
+                if ((r = prepare_trace(d, s, k.trace)))
+                        return r;
+        }
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
-        cudaEventRecord(e0, d.stream);
-        const void * fn = kernel_alm_grid(g_exact);
-        if ((r = launch_coop(fn, d.grid_blocks, &k, d.slots, d.stream)))
-                return r;
-        cudaEventRecord(e1, d.stream);
-        ACD_CUDA_TRY(cudaStreamSynchronize(d.stream), ACDALM_ECUDA);
         float ms = 0;
+        {
+                NvtxRange kr("acdalm solve kernel");
+                cudaEventRecord(e0, d.stream);
+                const void * fn = kernel_alm_grid(g_exact);
+                int launched = 0;
+                if ((r = launch_coop(fn, d.grid_blocks, &k, d.slots, d.stream, &launched)))
+                        return r;
+                cudaEventRecord(e1, d.stream);
+                ACD_CUDA_TRY(cudaStreamSynchronize(d.stream), ACDALM_ECUDA);
+                if (k.trace.rec) {
+                        d.trace_ctas = (size_t)launched;
+                        d.trace_count = k.trace.count;
+                }
+        }
         cudaEventElapsedTime(&ms, e0, e1);
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
+        NvtxRange down("acdalm download");
         return alm_finish(d, k, x, lam, log, diag3, w_out, c_out, st, ms * 1e-3);
 }
 

@@ -101,6 +101,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.alm_set_kkt_tolerance.argtypes = [_vp, C.c_double]
     L.alm_set_inner_budget.argtypes = [_vp, C.c_uint64]
     L.alm_last_stats.argtypes = [_vp, C.POINTER(Stats)]
+    L.alm_set_trace.argtypes = [_vp, C.c_uint64, C.c_uint64]
+    L.alm_trace_copy.argtypes = [_vp, _vp, _sz, C.POINTER(_sz), C.POINTER(_sz)]
     L.approx_last_stats.argtypes = [_vp, C.POINTER(Stats)]
     L.alm_stream.restype = _vp
     L.alm_stream.argtypes = [_vp]
@@ -381,6 +383,20 @@ class Alm:
         s = Stats()
         lib().alm_last_stats(self.h, C.byref(s))
         return s.as_dict()
+
+    def set_trace(self, first: int, count: int):
+        check(lib().alm_set_trace(self.h, first, count), "alm_set_trace")
+
+    def trace(self) -> np.ndarray:
+        """Phase stamps of the last traced solve: [reduction, cta, phase] ns."""
+        ctas, count = _sz(), _sz()
+        check(lib().alm_trace_copy(self.h, None, 0, C.byref(ctas), C.byref(count)),
+              "alm_trace_copy")
+        out = np.zeros(ctas.value * count.value * 3, np.uint64)
+        if out.size:
+            check(lib().alm_trace_copy(self.h, out.ctypes.data_as(_vp), out.size,
+                                       C.byref(ctas), C.byref(count)), "alm_trace_copy")
+        return out.reshape(count.value, ctas.value, 3)
 
     def stream(self) -> int:
         return lib().alm_stream(self.h) or 0

@@ -441,6 +441,9 @@ def main():
     ap.add_argument("--profile-solve", type=int, default=0,
                     help="run one ALM solve capped at this many inner iterations and exit "
                          "(the command the ncu captures use)")
+    ap.add_argument("--trace", type=int, default=0,
+                    help="trace this many grid-team reductions (from the 2,001st) of one "
+                         "solve capped at 3,000 inner iterations; print the phase breakdown")
     ap.add_argument("--ref-iters", type=int, default=4000,
                     help="APPROX iterations each CPU sample times (about 6 s on 16 cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -493,6 +496,9 @@ def main():
 
     lib = importlib.import_module("acd-alm_gb300.lib")
     L = lib.lib()
+    if args.trace:
+        trace_solve(args, lib, lp)
+        return
     if args.profile_solve:
         m = lib.Matrix(lp)
         alm = lib.Alm(m, lp)
@@ -627,6 +633,54 @@ def main():
     m.free()
     if dist:
         dist.destroy_process_group()
+
+
+def trace_solve(args, lib, lp, first=2001):
+    """--trace N: one solve of the workload capped at 3,000 inner iterations,
+    with the grid team's reductions first .. first + N - 1 traced (two per
+    steady-state inner iteration: the A' pass and the A pass); prints where
+    the time of an iteration goes.  Times in ns, from %globaltimer."""
+    m = lib.Matrix(lp)
+    alm = lib.Alm(m, lp)
+    if args.precision == "mixed":
+        alm.set_precision(lib.PRECISION_MIXED)
+    alm.set_inner_budget(3000)
+    alm.set_trace(first, args.trace)
+    alm.solve(1000)
+    st = alm.stats()
+    t = alm.trace().astype(np.int64)          # [reduction, cta, phase]
+    alm.free()
+    m.free()
+    ok = (t > 0).all(axis=(1, 2))
+    es = [e for e in range(1, t.shape[0]) if ok[e] and ok[e - 1]]
+    enter, ready, leave = t[:, :, 0], t[:, :, 1], t[:, :, 2]
+    pas = np.array([enter[e] - leave[e - 1] for e in es])       # per CTA: its warp 0's pass
+    whole = np.array([ready[e] - leave[e - 1] for e in es])     # per CTA: the CTA's pass
+    last = np.array([ready[e].max() for e in es])
+    after = np.array([leave[e] - last[i] for i, e in enumerate(es)])
+    blk = np.array([ready[e] - enter[e] for e in es])
+    cycle = np.array([leave[e].max() - leave[e - 1].max() for e in es])
+
+    def st_(a):
+        return {"mean": float(a.mean()), "p50": float(np.median(a)), "max": float(a.max())}
+
+    out = {"trace": args.trace, "workload": args.workload, "precision": args.precision,
+           "ctas": int(t.shape[1]), "inner_iterations": st["inner_iterations"],
+           "us_per_inner_iteration": st["seconds"] / max(st["inner_iterations"], 1) * 1e6,
+           "reduction_cycle_ns": st_(cycle),
+           "cta_pass_ns": {"mean_over_ctas": st_(whole.mean(1)), "max_over_ctas": st_(whole.max(1))},
+           "warp0_pass_ns": st_(pas), "block_reduce_ns": st_(blk),
+           "leave_after_last_cta_ready_ns": st_(after)}
+    for par in (0, 1):
+        sel = [i for i, e in enumerate(es) if (e + first) % 2 == par]
+        if sel:
+            out[f"reductions_{par}_mod_2"] = {"cycle": st_(cycle[sel]),
+                                              "cta_pass_max": st_(whole[sel].max(1)),
+                                              "cta_pass_mean": st_(whole[sel].mean(1))}
+    slow = whole.mean(0)
+    out["slowest_ctas"] = [int(i) for i in np.argsort(-slow)[:8]]
+    out["cta_pass_mean_ns_by_cta"] = {"max": float(slow.max()), "min": float(slow.min())}
+    print(json.dumps(out), flush=True)
 
 
 def _alm_weight(L, alm):

@@ -86,6 +86,18 @@ typedef struct acdalm_stats {
 int alm_last_stats(struct alm *, acdalm_stats_t * out);
 int approx_last_stats(struct approx *, acdalm_stats_t * out);
 
+/* Tracing of the whole-GPU solve (alm_solve): when count > 0, each CTA of
+ * the next solves records, for the team reductions first .. first + count -
+ * 1 (counted from 1 in each solve; two per steady-state inner iteration),
+ * three %globaltimer stamps (ns): entering the reduction (its warp 0's part
+ * of the pass done), after its block reduction (the whole CTA done), and
+ * leaving it (every CTA's partials summed).  alm_trace_copy writes them as
+ * out[((e - first) * ctas + cta) * 3 + phase] (cap values at most) and the
+ * sizes to *ctas and *count; with out NULL it reports the sizes only.
+ * count = 0 turns tracing off.  No reference counterpart. */
+int alm_set_trace(struct alm *, uint64_t first, uint64_t count);
+int alm_trace_copy(struct alm *, uint64_t * out, size_t cap, size_t * ctas, size_t * count);
+
 /* Rounding of the solver kernels: 0 (default) fused multiply-adds; 1 the
  * reference's separate rounding of every product and sum, which makes the
  * per-element results of each pass bit-identical to the reference's (the

@@ -102,6 +102,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.alm_set_inner_budget.argtypes = [_vp, C.c_uint64]
     L.alm_last_stats.argtypes = [_vp, C.POINTER(Stats)]
     L.alm_set_trace.argtypes = [_vp, C.c_uint64, C.c_uint64]
+    L.acdalm_autotune.argtypes = [_vp, _sz, C.POINTER(C.c_int)]
     L.alm_trace_copy.argtypes = [_vp, _vp, _sz, C.POINTER(_sz), C.POINTER(_sz)]
     L.approx_last_stats.argtypes = [_vp, C.POINTER(Stats)]
     L.alm_stream.restype = _vp
@@ -383,6 +384,12 @@ class Alm:
         s = Stats()
         lib().alm_last_stats(self.h, C.byref(s))
         return s.as_dict()
+
+    def autotune(self, iterations: int = 300) -> int:
+        """acdalm_autotune: the step cap chosen for this instance's layout."""
+        chosen = C.c_int(-1)
+        check(lib().acdalm_autotune(self.h, iterations, C.byref(chosen)), "acdalm_autotune")
+        return chosen.value
 
     def set_trace(self, first: int, count: int):
         check(lib().alm_set_trace(self.h, first, count), "alm_set_trace")

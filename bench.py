@@ -447,6 +447,8 @@ def main():
     ap.add_argument("--ref-iters", type=int, default=4000,
                     help="APPROX iterations each CPU sample times (about 6 s on 16 cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default layout instead of acdalm_autotune's choice")
     ap.add_argument("--side-steps", type=int, default=2,
                     help="solves of the other precision form, reported beside the "
                          "headline (0 = none)")
@@ -515,6 +517,8 @@ def main():
     L.acdalm_launch_count.restype = __import__("ctypes").c_ulonglong
     m = lib.Matrix(lp)
     alm = lib.Alm(m, lp)
+    # the layout's step cap, picked by timing on this GPU (untimed set-up)
+    tuned = alm.autotune(300) if not args.no_autotune else None
     alm.set_kkt_tolerance(1e-6)
     if args.precision == "mixed":
         alm.set_precision(lib.PRECISION_MIXED)
@@ -618,6 +622,8 @@ def main():
                   "objective": k["objective"], "device_seconds": dev_s,
                   "wall_seconds": wall_s},
         "reference_solve": ref_rec,
+        "layout": {"max_steps": tuned, "chosen_by": "acdalm_autotune (300 APPROX iterations "
+                   "per candidate cap, before the warm-up)" if tuned is not None else "default"},
         "clocks": clk,
     }
     if ref_rec:

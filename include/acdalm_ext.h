@@ -86,6 +86,16 @@ typedef struct acdalm_stats {
 int alm_last_stats(struct alm *, acdalm_stats_t * out);
 int approx_last_stats(struct approx *, acdalm_stats_t * out);
 
+/* Autotuning of the whole-GPU solve (alm_solve): builds the instance's
+ * device layout with each candidate cap on the steps of a slice (0 = the
+ * plain width rule, 4, 8, 12, 16; more lanes per row for fewer steps), times
+ * `iterations` APPROX iterations of the instance with each, and keeps the
+ * fastest for its next solves (*chosen, may be NULL).  The choice is
+ * remembered for instances of the same size class (row, column and nonzero
+ * counts within half an octave), which then skip the timing.  Without it
+ * the cap is ACDALM_SELL_STEPS, else 8.  No reference counterpart. */
+int acdalm_autotune(struct alm *, size_t iterations, int * chosen);
+
 /* Tracing of the whole-GPU solve (alm_solve): when count > 0, each CTA of
  * the next solves records, for the team reductions first .. first + count -
  * 1 (counted from 1 in each solve; two per steady-state inner iteration),

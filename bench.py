@@ -248,6 +248,53 @@ def spmv_bench(args, lp):
     m.free()
 
 
+def layout_bench(args, lp):
+    """--layout: the reference's layouts of the workload's matrix (row and
+    column nonzero-count permutations, CSR of A and A' of the permuted
+    matrix: what approx_make's shadow copy holds) built on the host
+    (sparse_matrix_make with permute = 1) and on the GPU
+    (acdalm_layout_device, triplets resident in HBM), best of --spmv-reps."""
+    import ctypes
+    import torch
+    lib = importlib.import_module("acd-alm_gb300.lib")
+    L = lib.lib()
+    f = L.acdalm_layout_device
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_size_t] * 3 + [ctypes.c_void_p] * 3 + [ctypes.c_int] \
+        + [ctypes.c_void_p] * 9
+    host = []
+    for _ in range(min(3, args.spmv_reps)):
+        t0 = time.perf_counter()
+        mm = lib.Matrix(lp, permute=True)
+        host.append(time.perf_counter() - t0)
+        mm.free()
+    i32 = lambda a: torch.tensor(np.ascontiguousarray(a, np.uint32).view(np.int32), device="cuda")
+    rows, cols = i32(lp.rows), i32(lp.cols)
+    vals = torch.tensor(np.ascontiguousarray(lp.vals), device="cuda")
+    z = lambda k, dt=torch.int32: torch.empty(max(k, 1), dtype=dt, device="cuda")
+    outs = [z(lp.nrows), z(lp.ncols), z(lp.nrows + 1), z(lp.nnz), z(lp.nnz, torch.float64),
+            z(lp.ncols + 1), z(lp.nnz), z(lp.nnz, torch.float64)]
+    stream = torch.cuda.current_stream()
+    dev = []
+    for rep in range(args.spmv_reps + 1):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r = f(lp.nrows, lp.ncols, lp.nnz, rows.data_ptr(), cols.data_ptr(), vals.data_ptr(), 1,
+              *[o.data_ptr() for o in outs], stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        lib.check(r, "acdalm_layout_device")
+        if rep:
+            dev.append(e0.elapsed_time(e1) * 1e-3)
+    print(json.dumps({"metric": "layout build seconds (permutations + CSR of A and A')",
+                      "workload": args.workload, "m": lp.nrows, "n": lp.ncols, "nnz": lp.nnz,
+                      "host_s": min(host), "gpu_s": min(dev), "speedup": min(host) / min(dev),
+                      "host_note": "sparse_matrix_make(permute=1) on one host thread",
+                      "gpu_note": "acdalm_layout_device, triplets resident, CUDA events"}),
+          flush=True)
+
+
 def bytes_per_iteration(lp, fp32: bool) -> float:
     """Algorithmic bytes of one steady-state APPROX iteration: one pass over
     A and one over A' (each nonzero's value and column read once), plus the
@@ -455,6 +502,8 @@ def main():
     ap.add_argument("--spmv", action="store_true",
                     help="time the device SpMV variants on the workload's matrix")
     ap.add_argument("--spmv-reps", type=int, default=10)
+    ap.add_argument("--layout", action="store_true",
+                    help="time the layout build (host vs GPU) on the workload's matrix")
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--stream-count", type=int, default=48)
     ap.add_argument("--stream-limit", type=float, default=900.0,
@@ -479,6 +528,9 @@ def main():
 
     if args.spmv:
         spmv_bench(args, lp)
+        return
+    if args.layout:
+        layout_bench(args, lp)
         return
     if args.workload == "batch":
         batch_bench(args)

@@ -217,6 +217,25 @@ struct sparse_matrix * acdalm_approx_permuted_matrix(struct approx * a);
 int acdalm_approx_step_sizes(struct approx * a, double * beta, double * v,
                              double * inv_v);
 
+/* ---- layouts built on the device ---- */
+/* The reference's layouts of a matrix built on the GPU from triplets
+ * already in DEVICE memory (rows, cols: u32; values: f64; distinct
+ * (row, column) pairs): with permute = 1 the nonzero-count permutations of
+ * rows and columns (spmv/permutation.c:63-125; row_idx, col_idx: new -> old,
+ * nrows and ncols entries), else the identity; and the CSR of A (ptr:
+ * nrows + 1, columns and vals: nnz) and of A' (ptr_t: ncols + 1, columns_t,
+ * vals_t) of the permuted matrix, ordered as spmv/spmv_csr.c:27-80 orders
+ * them.  Byte for byte what sparse_matrix_make(..., permute) holds
+ * (acdalm_perm_copy, acdalm_csr_copy).  All arrays are device memory; the
+ * work runs on `stream` (NULL = default) and the call returns when it is
+ * done.  Out-of-range triplets return ACDALM_EINVAL before anything is
+ * indexed by them.  No reference counterpart. */
+int acdalm_layout_device(size_t nrows, size_t ncols, size_t nnz, const uint32_t * rows,
+                         const uint32_t * cols, const double * values, int permute,
+                         uint32_t * row_idx, uint32_t * col_idx, uint32_t * ptr,
+                         uint32_t * columns, double * vals, uint32_t * ptr_t,
+                         uint32_t * columns_t, double * vals_t, void * stream);
+
 /* ---- binary instances ---- */
 /* The content of alm_read's text format (alm.h) in binary: the magic
  * "ACDALMB1", u64 nrows, ncols, nnz, then the matrix's rows, columns (u32)

@@ -274,8 +274,23 @@ struct alignas(128) CtlWord {
         unsigned v;
         unsigned pad[31];
 };
+// Phase timestamps of the grid team's reductions (optional): for the
+// reductions first .. first + count - 1 (counted from 1 in each launch), CTA
+// b's thread 0 records %globaltimer at kTracePhases points -- entering the
+// reduction (its warp 0's share of the pass done), after the block
+// reduction (the whole CTA done), and leaving it (every CTA's partials
+// summed) -- at rec[((e - first) * gridDim.x + b) * kTracePhases + phase].
+constexpr int kTracePhases = 3;
+struct alignas(128) TraceBuf {
+        unsigned long long * rec;  // nullptr: tracing off
+        unsigned first, count;
+};
+
 struct TeamCtl {
         CtlWord status_w;
+        // read by the grid team's thread 0 at each reduction, so tracing
+        // costs the solve no registers
+        TraceBuf trace;
 };
 
 // Reduction slots: per CTA and parity one 128-byte line holding a 64-bit tag
@@ -305,33 +320,23 @@ __device__ __forceinline__ void st_release_u64(unsigned long long * p, unsigned 
 // every CTA waits for all tags of this epoch and sums all lines itself in
 // CTA order -- so every thread gets the same bits, in about two L2 round
 // trips, with no counters and no fences.
-// Phase timestamps of the grid team's reductions (optional): for the
-// reductions first .. first + count - 1 (counted from 1 in each launch), CTA
-// b's thread 0 records %globaltimer at kTracePhases points -- entering the
-// reduction (its warp 0's share of the pass done), after the block
-// reduction (the whole CTA done), and leaving it (every CTA's partials
-// summed) -- at rec[((e - first) * gridDim.x + b) * kTracePhases + phase].
-constexpr int kTracePhases = 3;
-struct TraceBuf {
-        unsigned long long * rec;  // nullptr: tracing off
-        unsigned first, count;
-};
-
 struct GridTeam {
         TeamCtl * ctl;
         double * slots;   // [2][gridDim.x][kSlotStride]
         double * result;  // unused (kept for the launch interface)
         int parity;
         unsigned epoch;   // reductions passed (the same count in every CTA)
-        TraceBuf trace;
 
         __device__ void stamp(unsigned e, int phase) const
         {
-                if (trace.rec && threadIdx.x == 0) {
-                        unsigned i = e - trace.first;
-                        if (e >= trace.first && i < trace.count)
-                                trace.rec[((size_t)i * gridDim.x + blockIdx.x) * kTracePhases
-                                          + phase] = global_ns();
+                if (threadIdx.x == 0) {
+                        unsigned long long * rec = ctl->trace.rec;
+                        if (rec) {
+                                unsigned first = ctl->trace.first, i = e - first;
+                                if (e >= first && i < ctl->trace.count)
+                                        rec[((size_t)i * gridDim.x + blockIdx.x) * kTracePhases
+                                            + phase] = global_ns();
+                        }
                 }
         }
 

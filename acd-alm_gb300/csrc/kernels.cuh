@@ -30,13 +30,12 @@ struct AlmKernelArgs {
         double * slots;
         double * result;
         AlmOut * out;
-        TraceBuf trace;
 };
 
 template <bool Exact>
 __global__ void __launch_bounds__(kThreads, 2) alm_kernel(AlmKernelArgs k)
 {
-        GridTeam tm{k.ctl, k.slots, k.result, 0, 0u, k.trace};
+        GridTeam tm{k.ctl, k.slots, k.result, 0, 0u};
         Alm<GridTeam, Exact> alm(tm, k.P, k.W, k.log, k.M);
         AlmOut out;
         memset(&out, 0, sizeof(out));
@@ -64,13 +63,12 @@ struct ApproxKernelArgs {
         double * slots;
         double * result;
         ApproxOut * out;
-        TraceBuf trace;
 };
 
 template <bool Exact>
 __global__ void __launch_bounds__(kThreads, 2) approx_kernel(ApproxKernelArgs k)
 {
-        GridTeam tm{k.ctl, k.slots, k.result, 0, 0u, k.trace};
+        GridTeam tm{k.ctl, k.slots, k.result, 0, 0u};
         Approx<double, GridTeam, Exact> ap(tm, k.P, k.W, k.log);
         ApproxOut out;
         memset(&out, 0, sizeof(out));
@@ -210,7 +208,7 @@ struct Spg {
 template <bool Exact>
 __global__ void __launch_bounds__(kThreads, 2) mpg_kernel(ApproxKernelArgs k)
 {
-        GridTeam tm{k.ctl, k.slots, k.result, 0, 0u, k.trace};
+        GridTeam tm{k.ctl, k.slots, k.result, 0, 0u};
         Approx<double, GridTeam, Exact> ap(tm, k.P, k.W, k.log);
         Spg<GridTeam, Exact> spg(ap);
         ApproxOut out;

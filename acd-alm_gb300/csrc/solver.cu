@@ -722,12 +722,22 @@ int run_alm(DevInstance & d, const HostVectors & hv, size_t niter, double * x,
         NvtxRange solve_range("acdalm alm_solve");
         AlmKernelArgs k;
         int r;
+        bool traced = false;
+        unsigned trace_count = 0;
         {
                 NvtxRange up("acdalm upload");
                 if ((r = alm_prepare(d, hv, niter, x, lam, log != nullptr, s, lay, k)))
                         return r;
-                if ((r = prepare_trace(d, s, k.trace)))
+                TraceBuf trace;
+                if ((r = prepare_trace(d, s, trace)))
                         return r;
+                // after reset_ctl zeroed the control block (tracing off)
+                if (trace.rec)
+                        ACD_CUDA_TRY(cudaMemcpyAsync(&static_cast<TeamCtl *>(d.ctl)->trace, &trace,
+                                                     sizeof(trace), cudaMemcpyHostToDevice,
+                                                     d.stream), ACDALM_ECUDA);
+                traced = trace.rec != nullptr;
+                trace_count = trace.count;
         }
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0);
@@ -742,9 +752,9 @@ int run_alm(DevInstance & d, const HostVectors & hv, size_t niter, double * x,
                         return r;
                 cudaEventRecord(e1, d.stream);
                 ACD_CUDA_TRY(cudaStreamSynchronize(d.stream), ACDALM_ECUDA);
-                if (k.trace.rec) {
+                if (traced) {
                         d.trace_ctas = (size_t)launched;
-                        d.trace_count = k.trace.count;
+                        d.trace_count = trace_count;
                 }
         }
         cudaEventElapsedTime(&ms, e0, e1);

@@ -320,16 +320,19 @@ __device__ __forceinline__ void st_release_u64(unsigned long long * p, unsigned 
 // every CTA waits for all tags of this epoch and sums all lines itself in
 // CTA order -- so every thread gets the same bits, in about two L2 round
 // trips, with no counters and no fences.
-struct GridTeam {
+template <bool Trace>
+struct GridTeamT {
         TeamCtl * ctl;
         double * slots;   // [2][gridDim.x][kSlotStride]
         double * result;  // unused (kept for the launch interface)
         int parity;
         unsigned epoch;   // reductions passed (the same count in every CTA)
 
+        // (compiled into the traced kernel only: even an untaken branch here
+        // costs the solve kernel registers)
         __device__ void stamp(unsigned e, int phase) const
         {
-                if (threadIdx.x == 0) {
+                if constexpr (Trace) if (threadIdx.x == 0) {
                         unsigned long long * rec = ctl->trace.rec;
                         if (rec) {
                                 unsigned first = ctl->trace.first, i = e - first;
@@ -496,6 +499,8 @@ struct GridTeam {
                 return reduce<1>(d, op);
         }
 };
+
+using GridTeam = GridTeamT<false>;
 
 // One CTA (one LP of a batch): barriers are __syncthreads, reductions stay
 // in shared memory, loads may use L1 (only this SM writes the LP's data).

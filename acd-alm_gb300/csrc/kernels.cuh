@@ -32,11 +32,13 @@ struct AlmKernelArgs {
         AlmOut * out;
 };
 
-template <bool Exact>
+// Trace: the grid team records phase timestamps (a separate instantiation,
+// so the untraced solve pays nothing for it).
+template <bool Exact, bool Trace = false>
 __global__ void __launch_bounds__(kThreads, 2) alm_kernel(AlmKernelArgs k)
 {
-        GridTeam tm{k.ctl, k.slots, k.result, 0, 0u};
-        Alm<GridTeam, Exact> alm(tm, k.P, k.W, k.log, k.M);
+        GridTeamT<Trace> tm{k.ctl, k.slots, k.result, 0, 0u};
+        Alm<GridTeamT<Trace>, Exact> alm(tm, k.P, k.W, k.log, k.M);
         AlmOut out;
         memset(&out, 0, sizeof(out));
         int r = alm.solve(k.a, k.x, k.lam, out);
@@ -288,6 +290,7 @@ __global__ void __launch_bounds__(kBatchThreads, 1) alm_cluster_kernel(AlmKernel
 // Kernel addresses, one translation unit each (k_*.cu).
 const void * kernel_alm_grid_fast();      // k_alm_grid.cu
 const void * kernel_alm_grid_exact();     // k_alm_grid_exact.cu
+const void * kernel_alm_grid_trace();     // k_alm_grid_trace.cu (fused, traced)
 const void * kernel_approx_grid(bool exact);  // k_approx_grid.cu
 const void * kernel_mpg_grid();               // k_approx_grid.cu
 const void * kernel_alm_single_fast();    // k_alm_block.cu

@@ -746,7 +746,8 @@ int run_alm(DevInstance & d, const HostVectors & hv, size_t niter, double * x,
         {
                 NvtxRange kr("acdalm solve kernel");
                 cudaEventRecord(e0, d.stream);
-                const void * fn = kernel_alm_grid(g_exact);
+                // the traced instantiation runs the fused form
+                const void * fn = traced ? kernel_alm_grid_trace() : kernel_alm_grid(g_exact);
                 int launched = 0;
                 if ((r = launch_coop(fn, d.grid_blocks, &k, d.slots, d.stream, &launched)))
                         return r;
@@ -1157,6 +1158,7 @@ void preload_solver_kernels()
                 cudaFuncGetAttributes(&a, kernel_alm_cluster(e));
         }
         cudaFuncGetAttributes(&a, kernel_mpg_grid());
+        cudaFuncGetAttributes(&a, kernel_alm_grid_trace());
 }
 
 }  // namespace acd

@@ -104,7 +104,9 @@ int acdalm_autotune(struct alm *, size_t iterations, int * chosen);
  * leaving it (every CTA's partials summed).  alm_trace_copy writes them as
  * out[((e - first) * ctas + cta) * 3 + phase] (cap values at most) and the
  * sizes to *ctas and *count; with out NULL it reports the sizes only.
- * count = 0 turns tracing off.  No reference counterpart. */
+ * count = 0 turns tracing off.  A traced solve runs a separately compiled
+ * kernel (fused multiply-adds), so untraced solves pay nothing for the
+ * feature.  No reference counterpart. */
 int alm_set_trace(struct alm *, uint64_t first, uint64_t count);
 int alm_trace_copy(struct alm *, uint64_t * out, size_t cap, size_t * ctas, size_t * count);
 

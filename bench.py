@@ -170,6 +170,13 @@ def stream_bench(args):
     th.join()
     srv.close()
     lat = np.array([v[4] for v in done.values()])
+    msz = np.array([int(sizes[sub[r]]) for r in done if r in sub])
+    lat_m = np.array([done[r][4] for r in done if r in sub])
+    by_m = {}
+    for name, sel in (("m<=20000", msz <= 20000), ("m>20000", msz > 20000)):
+        if sel.any():
+            by_m[name] = {"count": int(sel.sum()), "p50_s": float(np.percentile(lat_m[sel], 50)),
+                          "p99_s": float(np.percentile(lat_m[sel], 99))}
     kk = [v[3]["rel_kkt"] for v in done.values()]
     sample = [lps[i] for i in range(0, k, max(1, k // args.plain_sample))]
     plain = _plain_fp64_rate(lib, sample)
@@ -181,6 +188,9 @@ def stream_bench(args):
                                  "m": "log-uniform [500, 200000]", "n": "2m",
                                  "arrivals": "Poisson 2000/s", "max_m": int(sizes.max())},
                       "completed": len(done), "solved": sum(1 for v in done.values() if v[0] == 0),
+                      "arrival_span_s": float(arrivals[-1]) if k else 0.0,
+                      "latency_by_size": by_m,
+                      "requests": k, "precision": args.precision,
                       "wall_s": wall, "p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
                       "p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
                       "rel_kkt_device_max": max(kk) if kk else None,
@@ -460,10 +470,10 @@ METRIC = "LPs/sec to 1e-6 relative KKT"
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one FP64 inner
 # iteration of the mid LP's solve kernel, from one ncu capture of
-# `bench.py --profile-solve 3000 --precision fp64` (3,000 FP64 iterations;
+# `bench.py --profile-solve 3000` (3,000 FP64 iterations;
 # profiles/alm_kernel_mid_traffic.md).  FP32 iterations are scaled by their
 # algorithmic bytes.
-MID_DRAM_BYTES_PER_FP64_ITER = (7724266240 + 3569961216) / 3000 * 85470432.0 / 52380288.0
+MID_DRAM_BYTES_PER_FP64_ITER = (13897512448 + 5532968192) / 3000
 TRAFFIC_NOTE = ("ncu DRAM bytes per launch, scaled from a 3,000-iteration capture of the "
                 "same kernel; the instance stays in L2, so traffic is far below the "
                 "algorithmic bytes")

@@ -33,6 +33,8 @@ constexpr unsigned long long kWaitLimitNs = 20ull * 1000000000ull;
 constexpr int kStatusTimeout = -2;                   // ACDALM_ETIMEOUT
 constexpr int kStatusNonFinite = -5;                 // ACDALM_ENONFINITE
 constexpr int kStatusTimeLimit = -7;                 // ACDALM_ETIMELIMIT
+constexpr int kStatusInternal = -4;                  // ACDALM_EINVAL: an internal
+                                                     // invariant did not hold
 
 enum RedOp { RED_SUM = 0, RED_MAX = 1, RED_MIN = 2 };
 
@@ -951,7 +953,7 @@ __device__ __forceinline__ T finish_row(T acc, int shift, int width)
 // One row sum of a SELL slice: sum_k A_k x[col_k] for the row of this lane
 // (valid in the row's lead lane).  Exact: the row's sequential order with
 // rounded products and sums; otherwise FMA chains per lane and a tree.
-template <bool Exact, int VEC, class Team, class V, class T>
+template <bool Exact, int VEC, int XS, class Team, class V, class T>
 __device__ __forceinline__ T slice_row_sum(const Team & tm, const SellDev<V> & op,
                                            const Slice & sl, const T * x, int lane)
 {
@@ -963,7 +965,7 @@ __device__ __forceinline__ T slice_row_sum(const Team & tm, const SellDev<V> & o
                         T p[VEC];
 #pragma unroll
                         for (int j = 0; j < VEC; j++)
-                                p[j] = mul_exact((T)q.a[j], tm.ld(x + q.c[j]));
+                                p[j] = mul_exact((T)q.a[j], tm.ld(x + XS * q.c[j]));
                         acc = in_order<VEC>(acc, p, sl.shift, lane);
                 }
                 return acc;
@@ -976,8 +978,8 @@ __device__ __forceinline__ T slice_row_sum(const Team & tm, const SellDev<V> & o
                         T x0[VEC], x1[VEC];
 #pragma unroll
                         for (int j = 0; j < VEC; j++) {
-                                x0[j] = tm.ld(x + q0.c[j]);
-                                x1[j] = tm.ld(x + q1.c[j]);
+                                x0[j] = tm.ld(x + XS * q0.c[j]);
+                                x1[j] = tm.ld(x + XS * q1.c[j]);
                         }
 #pragma unroll
                         for (int j = 0; j < VEC; j++) {
@@ -989,17 +991,17 @@ __device__ __forceinline__ T slice_row_sum(const Team & tm, const SellDev<V> & o
                         Chunk<VEC, V> q0 = team_chunk<VEC>(tm, op.col, op.val, at);
 #pragma unroll
                         for (int j = 0; j < VEC; j++)
-                                acc = madd<false>((T)q0.a[j], tm.ld(x + q0.c[j]), acc);
+                                acc = madd<false>((T)q0.a[j], tm.ld(x + XS * q0.c[j]), acc);
                 }
                 return finish_row(acc + acc2, sl.shift, (sl.steps * VEC) << sl.shift);
         }
 }
 
-// Row sums of one SELL operator applied to x.  For every live row, in the
-// row's lead lane: pv = pre(row) is loaded before the row's entries (so the
-// epilogue's operands arrive while the row is summed), then
-// epi(row, sum, pv).
-template <bool Exact, class Team, class V, class T, class Pre, class Epi>
+// Row sums of one SELL operator applied to x (entry j of x at x[XS j]).
+// For every live row, in the row's lead lane: pv = pre(row) is loaded
+// before the row's entries (so the epilogue's operands arrive while the row
+// is summed), then epi(row, sum, pv).
+template <bool Exact, int XS = 1, class Team, class V, class T, class Pre, class Epi>
 __device__ __forceinline__ void sell_rows_1p(const Team & tm, const SellDev<V> & op,
                                              const T * x, Pre && pre, Epi && epi)
 {
@@ -1008,7 +1010,7 @@ __device__ __forceinline__ void sell_rows_1p(const Team & tm, const SellDev<V> &
                 bool live = sl.lead && sl.row < op.nrows;
                 auto pv = pre(live ? sl.row : -1);
                 T acc = by_width(sl, [&](auto w) {
-                        return slice_row_sum<Exact, decltype(w)::value>(tm, op, sl, x, lane);
+                        return slice_row_sum<Exact, decltype(w)::value, XS>(tm, op, sl, x, lane);
                 });
                 if (live)
                         epi(sl.row, acc, pv);
@@ -1019,13 +1021,13 @@ struct NoPre {
         __device__ int operator()(int) const { return 0; }
 };
 
-// Row sums of one SELL operator applied to x; calls epi(row, sum) in the
-// row's lead lane for every live row.
-template <bool Exact, class Team, class V, class T, class Epi>
+// Row sums of one SELL operator applied to x (entry j at x[XS j]); calls
+// epi(row, sum) in the row's lead lane for every live row.
+template <bool Exact, int XS = 1, class Team, class V, class T, class Epi>
 __device__ __forceinline__ void sell_rows_1(const Team & tm, const SellDev<V> & op,
                                             const T * x, Epi && epi)
 {
-        sell_rows_1p<Exact>(tm, op, x, NoPre(), [&](int r, T acc, int) { epi(r, acc); });
+        sell_rows_1p<Exact, XS>(tm, op, x, NoPre(), [&](int r, T acc, int) { epi(r, acc); });
 }
 
 // Two right-hand sides sharing one pass over the operator, with the same
@@ -1085,6 +1087,84 @@ __device__ __forceinline__ void sell_rows_2(const Team & tm, const SellDev<V> & 
 {
         sell_rows_2p<Exact>(tm, op, x0, x1, NoPre(),
                             [&](int r, T a0, T a1, int) { epi(r, a0, a1); });
+}
+
+// Two values stored side by side (16 bytes for doubles, 8 for floats).
+template <class T>
+struct PairOf;
+template <>
+struct PairOf<double> {
+        typedef double2 type;
+};
+template <>
+struct PairOf<float> {
+        typedef float2 type;
+};
+
+// p[0] = a, p[1] = b in one store (p aligned to the pair's size).
+template <class T>
+__device__ __forceinline__ void store_pair(T * p, T a, T b)
+{
+        typedef typename PairOf<T>::type P2;
+        P2 v;
+        v.x = a;
+        v.y = b;
+        *reinterpret_cast<P2 *>(p) = v;
+}
+
+// Two right-hand sides stored as one interleaved pair vector (entry j of the
+// first at xy[2 j], of the second at xy[2 j + 1]; xy aligned to a pair):
+// each entry of the operator fetches both with one gather.  Same sums and
+// the same pre / epi protocol as sell_rows_2p: epi(row, sum0, sum1, pv).
+template <bool Exact, class Team, class V, class T, class Pre, class Epi>
+__device__ __forceinline__ void sell_rows_pair(const Team & tm, const SellDev<V> & op,
+                                               const T * xy, Pre && pre, Epi && epi)
+{
+        typedef typename PairOf<T>::type P2;
+        const P2 * xp = reinterpret_cast<const P2 *>(xy);
+        int lane = threadIdx.x & 31;
+        for_each_slice_of(tm, op, lane, [&](const Slice & sl) {
+                bool live = sl.lead && sl.row < op.nrows;
+                auto pv = pre(live ? sl.row : -1);
+                T a0 = 0, a1 = 0;
+                by_width(sl, [&](auto w) {
+                        constexpr int VEC = decltype(w)::value;
+                        int64_t at = sl.base + VEC * lane;
+                        if constexpr (Exact) {
+                                for (int t = 0; t < sl.steps; t++, at += 32 * VEC) {
+                                        Chunk<VEC, V> q = team_chunk<VEC>(tm, op.col, op.val, at);
+                                        T p[VEC], r[VEC];
+#pragma unroll
+                                        for (int j = 0; j < VEC; j++) {
+                                                P2 g = tm.ld(xp + q.c[j]);
+                                                p[j] = mul_exact((T)q.a[j], g.x);
+                                                r[j] = mul_exact((T)q.a[j], g.y);
+                                        }
+                                        a0 = in_order<VEC>(a0, p, sl.shift, lane);
+                                        a1 = in_order<VEC>(a1, r, sl.shift, lane);
+                                }
+                        } else {
+                                for (int t = 0; t < sl.steps; t++, at += 32 * VEC) {
+                                        Chunk<VEC, V> q = team_chunk<VEC>(tm, op.col, op.val, at);
+                                        P2 g[VEC];
+#pragma unroll
+                                        for (int j = 0; j < VEC; j++)
+                                                g[j] = tm.ld(xp + q.c[j]);
+#pragma unroll
+                                        for (int j = 0; j < VEC; j++) {
+                                                a0 = madd<false>((T)q.a[j], g[j].x, a0);
+                                                a1 = madd<false>((T)q.a[j], g[j].y, a1);
+                                        }
+                                }
+                                int width = (sl.steps * VEC) << sl.shift;
+                                a0 = finish_row(a0, sl.shift, width);
+                                a1 = finish_row(a1, sl.shift, width);
+                        }
+                        return 0;
+                });
+                if (live)
+                        epi(sl.row, a0, a1, pv);
+        });
 }
 
 }  // namespace acd

@@ -43,8 +43,9 @@ struct DevInstance {
                * v = nullptr, * inv_v = nullptr, * x = nullptr;
         // workspace (n): z, zp, x, g, g2, prev, prev_alt, alt_x, u
         double * wn[9] = {};
-        // workspace (m): y_viol, z_viol, zp_viol, x_viol, alt_xv, alt_yv
-        double * wm[6] = {};
+        // workspace (2m each): violation vectors in interleaved pairs --
+        // (z, y), (zp, the y its A pass writes), (x, x's spare)
+        double * wm[3] = {};
 
         // team control, reduction slots, log ring, outputs
         void * ctl = nullptr;          // TeamCtl
@@ -69,7 +70,7 @@ struct DevInstance {
         float * cf = nullptr, * lf = nullptr, * uf = nullptr,       // n
               * vf = nullptr, * ivf = nullptr, * d = nullptr;
         float * wnf[9] = {};
-        float * wmf[6] = {};
+        float * wmf[3] = {};
 
         int create(const DeviceLayout & lay);
         int ensure_f32(const DeviceLayout & lay);
@@ -190,7 +191,7 @@ struct ScratchSolve {
         int * log_count = nullptr;
         double * v = nullptr, * inv_v = nullptr, * xd = nullptr;
         double * wn[9] = {};
-        double * wm[6] = {};
+        double * wm[3] = {};  // 2m each, as DevInstance::wm
 };
 // Bytes of the control region of a ScratchSolve for max_blocks CTAs
 // (everything but the vectors).

@@ -99,7 +99,7 @@ struct Spg {
                 auto & P = ap.P;
                 auto & W = ap.W;
                 // state (approx.c:531-539): x = P(x0), z = x, g = grad(x), g2 = g
-                Vec<double> x = {W.xx, W.xv, 0, NAN, NAN};
+                Vec<double> x = {W.xx, W.vx, 0, NAN, NAN};
                 double * z = W.zx;
                 double * g = W.g;
                 double * g2 = W.g2;
@@ -133,7 +133,7 @@ struct Spg {
                         double part[4] = {0, 0, 0, 0};
                         const int op[4] = {RED_SUM, RED_SUM, RED_SUM, RED_SUM};
                         {
-                                sell_rows_1<Exact>(tm, P.At, x.viol, [&](int j, double s) {
+                                sell_rows_1<Exact, kViolStride>(tm, P.At, x.viol, [&](int j, double s) {
                                         double gj = s + tm.ld(P.c + j);
                                         g[j] = gj;
                                         double xj = tm.ld(x.x + j);

@@ -178,7 +178,7 @@ int upload_gather(DevInstance & d, double * dst, const double * src,
                 src = tmp.data();
         }
         // staged through the instance's spare buffer of that length
-        double * tmpdev = (len <= d.n) ? d.wn[8] : d.wm[5];
+        double * tmpdev = (len <= d.n) ? d.wn[8] : d.wm[2];
         ACD_CUDA_TRY(cudaMemcpyAsync(tmpdev, src, len * sizeof(double),
                                      cudaMemcpyHostToDevice, d.stream), ACDALM_ECUDA);
         gather_kernel<<<std::min(1024, (len + 255) / 256), 256, 0, d.stream>>>(
@@ -195,7 +195,7 @@ int download_scatter(DevInstance & d, double * dst, const double * src,
 {
         if (len == 0)
                 return 0;
-        double * tmpdev = (len <= d.n) ? d.wn[8] : d.wm[5];
+        double * tmpdev = (len <= d.n) ? d.wn[8] : d.wm[2];
         scatter_kernel<<<std::min(1024, (len + 255) / 256), 256, 0, d.stream>>>(
                 tmpdev, src, map, len);
         count_launch();
@@ -236,12 +236,9 @@ InnerWork<double> work_of(DevInstance & d)
         W.prev_alt = d.wn[6];
         W.alt_x = d.wn[7];
         W.ux = d.wn[8];
-        W.yv = d.wm[0];
-        W.zv = d.wm[1];
-        W.zpv = d.wm[2];
-        W.xv = d.wm[3];
-        W.alt_xv = d.wm[4];
-        W.alt_yv = d.wm[5];
+        W.vz = d.wm[0];
+        W.vzp = d.wm[1];
+        W.vx = d.wm[2];
         return W;
 }
 
@@ -344,7 +341,7 @@ int DevInstance::create(const DeviceLayout & lay)
         total += rounded((lay.at.ptr.size()) * 8) + rounded(sat * 4) + rounded(eat * 4) + rounded(eat * 8);
         total += rounded(mm * 4) + rounded(nn * 4) + rounded(mm * 8);
         total += 6 * rounded(mm * 8) + 7 * rounded(nn * 8);
-        total += 9 * rounded(nn * 8) + 6 * rounded(mm * 8);
+        total += 9 * rounded(nn * 8) + 3 * rounded(mm * 16);
         total += rounded(sizeof(TeamCtl)) + rounded(2 * (size_t)blocks * kSlotStride * 8)
                 + rounded(2 * kRedMax * 8);
         log_cap = kLogCap;
@@ -389,7 +386,7 @@ int DevInstance::create(const DeviceLayout & lay)
         for (auto & q : wn)
                 q = carve<double>(p, nn);
         for (auto & q : wm)
-                q = carve<double>(p, mm);
+                q = carve<double>(p, 2 * mm);
         ctl = carve<TeamCtl>(p, 1);
         slots = carve<double>(p, 2 * (size_t)blocks * kSlotStride);
         result = carve<double>(p, 2 * kRedMax);
@@ -426,11 +423,11 @@ size_t DevInstance::footprint(const DeviceLayout & lay, bool mixed)
         total += rounded((lay.at.ptr.size()) * 8) + rounded(sat * 4) + rounded(eat * 4) + rounded(eat * 8);
         total += rounded(mm * 4) + rounded(nn * 4) + rounded(mm * 8);
         total += 6 * rounded(mm * 8) + 7 * rounded(nn * 8);
-        total += 9 * rounded(nn * 8) + 6 * rounded(mm * 8);
+        total += 9 * rounded(nn * 8) + 3 * rounded(mm * 16);
         total += (size_t)2 << 20;  // control, slots, log ring, outputs (bounded)
         if (mixed)
                 total += rounded(ea * 4) + rounded(eat * 4) + 2 * rounded(mm * 4) + 15 * rounded(nn * 4)
-                        + 6 * rounded(mm * 4);
+                        + 3 * rounded(mm * 8);
         return total;
 }
 
@@ -442,7 +439,7 @@ int DevInstance::ensure_f32(const DeviceLayout & lay)
         size_t mm = std::max(m, 1), nn = std::max(n, 1);
         size_t total = rounded(std::max<size_t>(ea, 1) * 4) + rounded(std::max<size_t>(eat, 1) * 4)
                 + 2 * rounded(mm * 4) + 6 * rounded(nn * 4) + 9 * rounded(nn * 4)
-                + 6 * rounded(mm * 4);
+                + 3 * rounded(mm * 8);
         cudaError_t e = cudaMallocAsync(&mem32, total, stream);
         if (e != cudaSuccess) {
                 mem32 = nullptr;
@@ -465,7 +462,7 @@ int DevInstance::ensure_f32(const DeviceLayout & lay)
         for (auto & q : wnf)
                 q = carve<float>(p, nn);
         for (auto & q : wmf)
-                q = carve<float>(p, mm);
+                q = carve<float>(p, 2 * mm);
         ACD_CUDA_TRY(cudaMemsetAsync(mem32, 0, total, stream), ACDALM_ECUDA);
         std::vector<float> tmp(lay.a.val.begin(), lay.a.val.end());
         if (ea)
@@ -606,12 +603,9 @@ static int alm_prepare(DevInstance & d, const HostVectors & hv, size_t niter, do
                 Wf.prev_alt = d.wnf[6];
                 Wf.alt_x = d.wnf[7];
                 Wf.ux = d.wnf[8];
-                Wf.yv = d.wmf[0];
-                Wf.zv = d.wmf[1];
-                Wf.zpv = d.wmf[2];
-                Wf.xv = d.wmf[3];
-                Wf.alt_xv = d.wmf[4];
-                Wf.alt_yv = d.wmf[5];
+                Wf.vz = d.wmf[0];
+                Wf.vzp = d.wmf[1];
+                Wf.vx = d.wmf[2];
                 k.M.Wf = Wf;
         }
         k.x = d.x;
@@ -1072,12 +1066,9 @@ int run_approx_scratch(DevInstance & d, const HostVectors & hv, double * x_dev,
         W.prev_alt = s.wn[6];
         W.alt_x = s.wn[7];
         W.ux = s.wn[8];
-        W.yv = s.wm[0];
-        W.zv = s.wm[1];
-        W.zpv = s.wm[2];
-        W.xv = s.wm[3];
-        W.alt_xv = s.wm[4];
-        W.alt_yv = s.wm[5];
+        W.vz = s.wm[0];
+        W.vzp = s.wm[1];
+        W.vx = s.wm[2];
         k.W = W;
         k.log = {nullptr, 0, s.log_count};
         k.a.niter = (long long)std::min<size_t>(niter, (size_t)1 << 62);

@@ -48,10 +48,22 @@ struct InnerProblem {
         const T * inv_v;
 };
 
+// Violation vectors (m entries, w (A x - b) at some x) are stored in
+// interleaved pairs: entry i of a pair's first vector at [2 i], of its
+// second at [2 i + 1].  z's violation and y's always share a pair (z first),
+// because the A pass that computes zp's violation also computes the next
+// y's and writes both halves of zp's pair; the A' pass of the two-gradient
+// step then fetches both right-hand sides of column j with one 16-byte
+// (8-byte in FP32) gather instead of two.  x's violation and its
+// speculative successor share the third pair.  A vector's pointer is the
+// address of its entry 0; entry i is at [kViolStride * i].
+constexpr int kViolStride = 2;
+
 template <class T>
 struct InnerWork {
         T * zx, * zpx, * xx, * g, * g2, * prev, * prev_alt, * alt_x, * ux;  // n
-        T * yv, * zv, * zpv, * xv, * alt_xv, * alt_yv;                       // m
+        T * vz, * vzp, * vx;  // violation pairs, 2m each: (z, y), (zp, -), (x, -)
+        T * alt_xv;           // x's spare half (set by Approx::solve)
 };
 
 struct InnerArgs {
@@ -199,8 +211,10 @@ struct Approx {
                 Acc part[5] = {};
                 const int op[5] = {RED_SUM, RED_SUM, RED_SUM, RED_SUM, RED_MAX};
                 const T ts = T(1) - th, tt = th, ns = T(1) - nth, nt = nth;
+                constexpr int S = kViolStride;
+                // with the momentum update, v is zp: the next y's violation
+                // goes to the second half of v's pair, beside v's own
                 T * xvw = (linterp == 2) ? W.alt_xv : x.viol;
-                T * yvw = (linterp == 2) ? W.alt_yv : y.viol;
                 T * xxw = (linterp == 2) ? W.alt_x : x.x;
                 const T * xvr = x.viol;
                 const T * xxr = x.x;
@@ -213,19 +227,21 @@ struct Approx {
                                 q.b = tm.ld(P.b + i);
                                 q.w = tm.ld(P.w + i);
                                 if (linterp)
-                                        q.xv = tm.ld(xvr + i);
+                                        q.xv = tm.ld(xvr + S * i);
                         }
                         return q;
                 };
-                sell_rows_1p<Exact>(tm, P.A, v.x, pre, [&](int i, T ax, const RowPre & q) {
+                sell_rows_1p<Exact, 1>(tm, P.A, v.x, pre, [&](int i, T ax, const RowPre & q) {
                         T r = ax - q.b;
                         T s = mul<Exact>(q.w, r);
-                        v.viol[i] = s;
                         acc_prod(part[0], s, r);
                         if (linterp) {
                                 T xv = lerp2<Exact>(ts, q.xv, tt, s);
-                                yvw[i] = lerp2<Exact>(ns, xv, nt, s);
-                                xvw[i] = xv;
+                                T yv = lerp2<Exact>(ns, xv, nt, s);
+                                store_pair(v.viol + S * i, s, yv);
+                                xvw[S * i] = xv;
+                        } else {
+                                v.viol[S * i] = s;
                         }
                 });
                 if (linterp || want_cx || want_delta) {
@@ -332,13 +348,18 @@ struct Approx {
                                 acc_prod(part[4], cj, zj);
                         acc_prod(part[5], cj, trial);
                 };
-                if (two)
-                        sell_rows_2p<Exact>(tm, P.At, z.viol, y.viol, pre, epi);
-                else
-                        sell_rows_1p<Exact>(tm, P.At, y.viol, pre,
-                                            [&](int j, T g1, const ColPre & q) {
-                                                    epi(j, (T)0, g1, q);
-                                            });
+                if (two) {
+                        if (y.viol != z.viol + 1) {  // the pairing invariant
+                                tm.fail(kStatusInternal);
+                                return false;
+                        }
+                        sell_rows_pair<Exact>(tm, P.At, z.viol, pre, epi);
+                } else {
+                        sell_rows_1p<Exact, kViolStride>(tm, P.At, y.viol, pre,
+                                                         [&](int j, T g1, const ColPre & q) {
+                                                                 epi(j, (T)0, g1, q);
+                                                         });
+                }
                 double res[6];
                 if (!reduce(part, op, res))
                         return false;
@@ -360,7 +381,7 @@ struct Approx {
                 Acc part[2] = {};
                 const int op[2] = {RED_SUM, RED_SUM};
                 T * g = W.g;
-                sell_rows_1<Exact>(tm, P.At, v.viol, [&](int j, T a) {
+                sell_rows_1<Exact, kViolStride>(tm, P.At, v.viol, [&](int j, T a) {
                         T gj = a + tm.ld(P.c + j);
                         g[j] = gj;
                         T xj = tm.ld(v.x + j);
@@ -401,7 +422,7 @@ struct Approx {
                         acc_prod(part[0], gj, trial - zj);
                 };
                 if (need_grad) {
-                        sell_rows_1<Exact>(tm, P.At, z.viol, [&](int j, T a) {
+                        sell_rows_1<Exact, kViolStride>(tm, P.At, z.viol, [&](int j, T a) {
                                 T gj = a + tm.ld(P.c + j);
                                 g[j] = gj;
                                 body(j, gj);
@@ -423,9 +444,9 @@ struct Approx {
                 for (int j = tm.tid(); j < P.n; j += tm.nthreads())
                         x.x[j] = tm.ld(z.x + j);
                 for (int i = tm.tid(); i < P.m; i += tm.nthreads()) {
-                        T zi = tm.ld(z.viol + i);
-                        x.viol[i] = zi;
-                        y.viol[i] = zi;
+                        T zi = tm.ld(z.viol + kViolStride * i);
+                        x.viol[kViolStride * i] = zi;
+                        y.viol[kViolStride * i] = zi;
                 }
                 x.violp = y.violp = z.violp;
                 x.quad = y.quad = z.quad;
@@ -587,7 +608,7 @@ struct Approx {
                 }
                 if (!descent) {
                         if (!dd_valid) {  // unreachable: kept for safety
-                                tm.fail(-4);
+                                tm.fail(kStatusInternal);
                                 return -1;
                         }
                         if (dd > 0) {
@@ -602,13 +623,14 @@ struct Approx {
                 if (spec_valid && zp.violp) {
                         // adopt the momentum update computed speculatively
                         T * t = x.viol; x.viol = W.alt_xv; W.alt_xv = t;
-                        t = y.viol; y.viol = W.alt_yv; W.alt_yv = t;
                         t = x.x; x.x = W.alt_x; W.alt_x = t;
                 } else {
                         if (!violation(zp, 1, th, nth, false, false, nullptr, nullptr,
                                        nullptr))
                                 return -1;
                 }
+                // the next y's violation is the second half of zp's pair
+                y.viol = zp.viol + 1;
                 iteration += 1;
                 theta = nth;
                 y.value = x.value = NAN;
@@ -626,10 +648,11 @@ struct Approx {
                 t_start_ns = a.t_start_ns;
                 xbar = a.xbar;
                 // state init (approx.c:588-603)
-                y = {nullptr, W.yv, 0, NAN, NAN};
-                z = {W.zx, W.zv, 0, NAN, NAN};
-                zp = {W.zpx, W.zpv, 0, NAN, NAN};
-                x = {W.xx, W.xv, 0, NAN, NAN};
+                y = {nullptr, W.vz + 1, 0, NAN, NAN};
+                z = {W.zx, W.vz, 0, NAN, NAN};
+                zp = {W.zpx, W.vzp, 0, NAN, NAN};
+                x = {W.xx, W.vx, 0, NAN, NAN};
+                W.alt_xv = W.vx + 1;
                 iteration = 0;
                 theta = 1;
                 step_length = 1;
@@ -651,9 +674,8 @@ struct Approx {
                         W.prev[j] = v;
                 }
                 for (int i = tm.tid(); i < P.m; i += tm.nthreads()) {
-                        T v = tm.ld(x.viol + i);
-                        z.viol[i] = v;
-                        y.viol[i] = v;
+                        T v = tm.ld(x.viol + kViolStride * i);
+                        store_pair(z.viol + kViolStride * i, v, v);  // z and y
                 }
                 z.violp = y.violp = 1;
                 z.quad = y.quad = x.quad;

@@ -42,7 +42,7 @@ size_t rounded(size_t bytes)
 size_t scratch_bytes_needed(size_t n, size_t m)
 {
         return acd::scratch_control_bytes(kStaticBlocks) + 12 * rounded(n * 8)
-                + 6 * rounded(m * 8);
+                + 3 * rounded(m * 16);
 }
 
 // The device address of g_static_scratch on the current device, looked up
@@ -121,7 +121,7 @@ extern "C" int approx_solve_static(double * x, size_t n, approx_t * approx,
         for (auto & w : s.wn)
                 w = reinterpret_cast<double *>(carve(n * 8));
         for (auto & w : s.wm)
-                w = reinterpret_cast<double *>(carve(approx->nrhs * 8));
+                w = reinterpret_cast<double *>(carve(approx->nrhs * 16));
         acd::HostVectors hv;
         hv.b = approx->s_rhs.data();
         hv.w = approx->s_weight.data();

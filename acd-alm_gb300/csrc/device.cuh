@@ -295,37 +295,43 @@ struct TeamCtl {
         TraceBuf trace;
 };
 
-// Reduction slots: per CTA and parity one 128-byte line holding a 64-bit tag
-// (the barrier epoch that wrote it) and up to kRedMax values.
-constexpr int kSlotStride = 16;  // doubles per line
-// Lines a lane loads at once when it sums the CTAs' values: 12 covers 384
-// CTAs (2 per SM) in one round trip.
-constexpr int kSumWidth = 12;
-__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long * p)
+// Reduction slots: per CTA and parity one 128-byte line of 16 64-bit words.
+// Value k of a reduction is published as words 2k (low 32 bits of the
+// double) and 2k + 1 (high 32 bits), each word carrying the reduction's
+// epoch in its upper half: a reader that sees the current epoch in both
+// words holds that value, with no separate tag and no second round trip
+// (a naturally aligned 64-bit store is seen whole or not at all).
+constexpr int kSlotStride = 16;  // words per line
+// Lines a lane polls at once, per pass over the CTAs: 10 covers 320 CTAs
+// (2 per SM) in one pass; more CTAs take further passes.
+constexpr int kSumWidth = 10;
+__device__ __forceinline__ ulonglong2 ld_relaxed_u64x2(const unsigned long long * p)
 {
-        unsigned long long v;
-        asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+        ulonglong2 v;
+        asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];"
+                     : "=l"(v.x), "=l"(v.y) : "l"(p) : "memory");
         return v;
 }
-__device__ __forceinline__ void fence_acquire_gpu()
+__device__ __forceinline__ void fence_acq_rel_gpu()
 {
         asm volatile("fence.acq_rel.gpu;" ::: "memory");
 }
 
-__device__ __forceinline__ void st_release_u64(unsigned long long * p, unsigned long long v)
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long * p, unsigned long long v)
 {
-        asm volatile("st.release.gpu.global.u64 [%0], %1;" :: "l"(p), "l"(v) : "memory");
+        asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" :: "l"(p), "l"(v) : "memory");
 }
 
 // Every CTA of a cooperative launch.  team.reduce() is an all-gather: each
-// CTA publishes its partials in its own line with a release-stored tag, then
-// every CTA waits for all tags of this epoch and sums all lines itself in
-// CTA order -- so every thread gets the same bits, in about two L2 round
-// trips, with no counters and no fences.
+// CTA publishes its partials in its own line (epoch-tagged words, see
+// kSlotStride), then in every CTA warp k polls value k of all CTAs' lines
+// until every word shows the current epoch and sums them in CTA order -- so
+// every thread gets the same bits, about one L2 round trip after the last
+// CTA publishes, with no counters.
 template <bool Trace>
 struct GridTeamT {
         TeamCtl * ctl;
-        double * slots;   // [2][gridDim.x][kSlotStride]
+        double * slots;   // [2][gridDim.x][kSlotStride] words
         double * result;  // unused (kept for the launch interface)
         int parity;
         unsigned epoch;   // reductions passed (the same count in every CTA)
@@ -377,112 +383,108 @@ struct GridTeamT {
         template <int K, class P>
         __device__ bool reduce_to(const P (&v)[K], const int (&op)[K], double (&res)[K])
         {
-                __shared__ double tot[kRedMax];
-                __shared__ int bad;
+                static_assert(2 * K <= kSlotStride, "two words per value in a line");
+                __shared__ double tot[kRedMax];  // this CTA's totals
+                __shared__ double fin[kRedMax];  // the team's
+                __shared__ int bad[kRedMax];
                 stamp(epoch + 1, 0);
                 block_reduce<K>(v, op, tot);
                 epoch++;
                 stamp(epoch, 1);
                 const unsigned nb = gridDim.x;
-                double * lines = slots + (size_t)parity * nb * kSlotStride;
-                if (threadIdx.x == 0) {
-                        double * mine = lines + (size_t)blockIdx.x * kSlotStride;
-#pragma unroll
-                        for (int k = 0; k < K; k++)
-                                __stcg(mine + 1 + k, tot[k]);
-                        // release: this CTA's phase writes (ordered by the
-                        // block barrier) and the values above
-                        st_release_u64(reinterpret_cast<unsigned long long *>(mine), epoch);
+                unsigned long long * lines =
+                        reinterpret_cast<unsigned long long *>(slots) + (size_t)parity * nb * kSlotStride;
+                const unsigned long long tag = (unsigned long long)epoch << 32;
+                if (threadIdx.x < 2 * K) {
+                        unsigned long long bits =
+                                (unsigned long long)__double_as_longlong(tot[threadIdx.x >> 1]);
+                        unsigned half = (threadIdx.x & 1) ? (unsigned)(bits >> 32) : (unsigned)bits;
+                        // release: this CTA's phase writes, ordered before
+                        // this point by the block barrier
+                        fence_acq_rel_gpu();
+                        st_relaxed_u64(lines + (size_t)blockIdx.x * kSlotStride + threadIdx.x,
+                                       tag | half);
                 }
-                if (threadIdx.x < 32) {
-                        // wait for every CTA's tag of this epoch (bounded)
-                        int lane = threadIdx.x;
-                        unsigned pending = 0;
-                        for (unsigned q = 0, b = lane; b < nb; q++, b += 32)
-                                pending |= 1u << q;
-                        unsigned long long t0 = 0;
-                        int bad_local = 0;
-                        for (unsigned rounds = 0;; rounds++) {
-                                // relaxed loads, all in flight at once; one
-                                // acquire fence once every tag is seen
-                                for (unsigned q0 = 0; q0 * 32u < nb; q0 += 8) {
-                                        unsigned long long t[8];
-#pragma unroll
-                                        for (int j = 0; j < 8; j++) {
-                                                unsigned q = q0 + j, b = lane + 32u * q;
-                                                t[j] = (b < nb && ((pending >> q) & 1u))
-                                                        ? ld_relaxed_u64(reinterpret_cast<const unsigned long long *>(
-                                                                  lines + (size_t)b * kSlotStride))
-                                                        : epoch;
-                                        }
-#pragma unroll
-                                        for (int j = 0; j < 8; j++)
-                                                if (t[j] == epoch)
-                                                        pending &= ~(1u << (q0 + j));
-                                }
-                                if (!__any_sync(0xffffffffu, pending != 0))
-                                        break;
-                                __nanosleep(16);
-                                if ((rounds & 63) == 63) {
-                                        if (lane == 0) {
-                                                if (t0 == 0)
-                                                        t0 = global_ns();
-                                                if (ld_acquire_int(status()) != 0)
-                                                        bad_local = 1;
-                                                else if (global_ns() - t0 > kWaitLimitNs) {
-                                                        fail(kStatusTimeout);
-                                                        bad_local = 1;
-                                                }
-                                        }
-                                        if (__shfl_sync(0xffffffffu, bad_local, 0))
-                                                break;
-                                }
-                        }
-                        fence_acquire_gpu();
-                }
-                __syncthreads();
-                // warp k sums value k over all CTAs: each lane first issues all
-                // its loads (CTAs lane, lane+32, ...), then combines them in
-                // that fixed order, then a fixed shuffle tree
-                // the team's status word is read alongside the values (a
-                // relaxed load: it only has to show a failure eventually)
                 int status_now = 0;
-                if (threadIdx.x == 0)
-                        status_now = ld_relaxed_int(status());
-                {
-                        int lane = threadIdx.x & 31, wk = threadIdx.x >> 5;
-#pragma unroll
-                        for (int k = 0; k < K; k++) {
-                                if (wk != k)
-                                        continue;
-                                double idv = red_identity(op[k]);
+                if (threadIdx.x < 32 * K) {
+                        // warp k: value k of every CTA, lanes taking CTAs
+                        // lane, lane + 32, ...; combined in that fixed order,
+                        // then a fixed shuffle tree
+                        const int k = threadIdx.x >> 5, lane = threadIdx.x & 31;
+                        const double idv = red_identity(op[k]);
+                        double acc = idv;
+                        int broke = 0;
+                        unsigned long long t0 = 0;
+                        for (unsigned base = 0; base < nb && !broke; base += 32u * kSumWidth) {
                                 double vals[kSumWidth];
+                                unsigned pending = 0;
 #pragma unroll
                                 for (int q = 0; q < kSumWidth; q++) {
-                                        unsigned b = lane + 32u * q;
-                                        vals[q] = (b < nb) ? __ldcg(lines + (size_t)b * kSlotStride + 1 + k)
-                                                           : idv;
+                                        vals[q] = idv;
+                                        if (base + lane + 32u * q < nb)
+                                                pending |= 1u << q;
                                 }
-                                double acc = idv;
+                                for (unsigned rounds = 0;; rounds++) {
+                                        ulonglong2 w[kSumWidth];
+#pragma unroll
+                                        for (int q = 0; q < kSumWidth; q++) {
+                                                unsigned b = base + lane + 32u * q;
+                                                w[q] = ((pending >> q) & 1u)
+                                                        ? ld_relaxed_u64x2(lines + (size_t)b * kSlotStride + 2 * k)
+                                                        : make_ulonglong2(0, 0);
+                                        }
+#pragma unroll
+                                        for (int q = 0; q < kSumWidth; q++) {
+                                                if (((pending >> q) & 1u) &&
+                                                    (w[q].x & 0xffffffff00000000ull) == tag &&
+                                                    (w[q].y & 0xffffffff00000000ull) == tag) {
+                                                        pending &= ~(1u << q);
+                                                        vals[q] = __longlong_as_double(
+                                                                (long long)((w[q].y << 32) | (w[q].x & 0xffffffffull)));
+                                                }
+                                        }
+                                        if (!__any_sync(0xffffffffu, pending != 0))
+                                                break;
+                                        __nanosleep(16);
+                                        if ((rounds & 63) == 63) {
+                                                if (lane == 0) {
+                                                        if (t0 == 0)
+                                                                t0 = global_ns();
+                                                        if (ld_acquire_int(status()) != 0)
+                                                                broke = 1;
+                                                        else if (global_ns() - t0 > kWaitLimitNs) {
+                                                                fail(kStatusTimeout);
+                                                                broke = 1;
+                                                        }
+                                                }
+                                                broke = __shfl_sync(0xffffffffu, broke, 0);
+                                                if (broke)
+                                                        break;
+                                        }
+                                }
 #pragma unroll
                                 for (int q = 0; q < kSumWidth; q++)
                                         acc = red_combine(op[k], acc, vals[q]);
-                                for (unsigned b = lane + 32u * kSumWidth; b < nb; b += 32)
-                                        acc = red_combine(op[k], acc,
-                                                          __ldcg(lines + (size_t)b * kSlotStride + 1 + k));
-                                acc = warp_reduce(acc, op[k]);
-                                if (lane == 0)
-                                        tot[k] = acc;
                         }
+                        // acquire: the other CTAs' phase writes
+                        fence_acq_rel_gpu();
+                        acc = warp_reduce(acc, op[k]);
+                        if (lane == 0) {
+                                fin[k] = acc;
+                                bad[k] = broke;
+                        }
+                        // the team's status word, alongside (a relaxed load:
+                        // it only has to show a failure eventually)
+                        if (threadIdx.x == 0)
+                                status_now = ld_relaxed_int(status());
                 }
-                if (threadIdx.x == 0)
-                        bad = status_now != 0;
-                __syncthreads();
-                stamp(epoch, 2);
+                int b = __syncthreads_or(threadIdx.x == 0 && status_now != 0);
 #pragma unroll
-                for (int k = 0; k < K; k++)
-                        res[k] = tot[k];
-                int b = bad;
+                for (int k = 0; k < K; k++) {
+                        res[k] = fin[k];
+                        b |= bad[k];
+                }
+                stamp(epoch, 2);
                 parity ^= 1;
                 return !b;
         }

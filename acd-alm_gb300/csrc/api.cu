@@ -412,7 +412,8 @@ extern "C" {
 
 int alm_set_precision(struct alm * m, int mode)
 {
-        if (mode != ACDALM_PRECISION_FP64 && mode != ACDALM_PRECISION_MIXED) {
+        if (mode != ACDALM_PRECISION_FP64 && mode != ACDALM_PRECISION_MIXED &&
+            mode != ACDALM_PRECISION_AUTO) {
                 acd::set_error(ACDALM_EINVAL, "alm_set_precision: mode %d", mode);
                 return ACDALM_EINVAL;
         }

@@ -19,6 +19,7 @@ struct DevInstance {
         int m = 0, n = 0;
         int64_t nnz = 0;
         cudaStream_t stream = nullptr;
+        int priority = 0;  // of the stream create() makes (lower runs sooner)
         void * mem = nullptr;
         size_t bytes = 0;
 
@@ -90,10 +91,18 @@ struct HostVectors {
         const double * u = nullptr;       // n
 };
 
+// Whether an LP with nnz nonzeros runs FP32 inner iterations under an
+// ACDALM_PRECISION_* mode (AUTO: from kAutoMixedNnz nonzeros on).
+constexpr int64_t kAutoMixedNnz = 500000;
+inline bool mixed_for(int precision, int64_t nnz)
+{
+        return precision == 1 || (precision == 2 && nnz >= kAutoMixedNnz);
+}
+
 struct AlmSettings {
         unsigned long long inner_budget = 0;
         double kkt_tol = 0;
-        int precision = 0;
+        int precision = 0;  // ACDALM_PRECISION_*
         // grid-team reductions first .. first + count - 1 are traced
         unsigned trace_first = 0, trace_count = 0;
 };

@@ -9,7 +9,17 @@
 // a small LP, a thread-block cluster of up to 16 CTAs for a large one -- so
 // LPs that arrive while others are on the GPU run beside them.  Finished
 // solves are retired (results read back, device memory freed), which frees
-// budget for the next requests.  Every solve is the same computation whether
+// budget for the next requests.
+//
+// Admission packs the GPU's SMs: every solve holds `team` SMs (one CTA per
+// SM) until it ends, and a request is admitted only while the running
+// teams leave that many SMs free, so no admitted solve waits in the
+// hardware queue holding a slot.  Among built requests the one with the
+// most nonzeros that fits goes first (a large LP started late would set
+// the end of the whole stream); smaller ones fill SMs a larger one cannot
+// use yet, until that one has waited kBackfillSeconds, after which nothing
+// passes it.  Clusters run on high-priority streams: a cluster's CTAs must
+// all find room in one GPC at once.  Every solve is the same computation whether
 // it runs alone or in the mix (a fixed team, deterministic reductions).
 #include <cuda_runtime.h>
 
@@ -39,11 +49,15 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
+// How long a built request may be passed by smaller ones that fit the free
+// SMs before it blocks them (see the admission rule above).
+constexpr double kBackfillSeconds = 10.0;
+
 enum State { PENDING, BUILT, RUNNING, DONE, FAILED };
 
 struct Request {
         long long id = 0;
-        size_t m = 0, n = 0;
+        size_t m = 0, n = 0, nnz = 0;
         std::vector<uint32_t> rows, cols;
         std::vector<double> vals, rhs, linear, lower, upper, llo, lhi;
         sparse_matrix_t * matrix = nullptr;
@@ -56,7 +70,7 @@ struct Request {
         acd::SolveStats stats;
         int ret = 0;
         State state = PENDING;
-        Clock::time_point t_submit, t_admit, t_done;
+        Clock::time_point t_submit, t_built, t_admit, t_done;
 };
 
 }  // namespace
@@ -64,9 +78,12 @@ struct Request {
 struct acdalm_server {
         size_t budget = 0;         // device bytes for admitted instances
         int max_team = 16;         // largest cluster the device launches
+        int sms = 0;               // SMs of the device
+        int sms_busy = 0;          // SMs the running solves' teams hold
         size_t in_use = 0;
         int max_inflight = 0;
         int precision = 0;
+        int high_priority = 0;     // stream priority of cluster solves
         double kkt_tol = 1e-6;
         size_t niter = 1000;
         unsigned long long inner_budget = 0;
@@ -131,11 +148,16 @@ void build_one(acdalm_server_t * s, Request * r)
         r->alm->settings.kkt_tol = s->kkt_tol;
         r->alm->settings.precision = s->precision;
         r->alm->settings.inner_budget = s->inner_budget;
-        r->footprint = acd::DevInstance::footprint(a->lay, s->precision == 1);
+        r->footprint = acd::DevInstance::footprint(a->lay,
+                                                   acd::mixed_for(s->precision, a->lay.nnz));
         r->state = BUILT;
-        // keep arrival order: a request becomes admissible in id order
+        r->t_built = Clock::now();
+        // admission order: most nonzeros first, then arrival
+        auto before = [](const Request * p, const Request * q) {
+                return p->nnz != q->nnz ? p->nnz > q->nnz : p->id < q->id;
+        };
         auto it = s->built.begin();
-        while (it != s->built.end() && (*it)->id < r->id)
+        while (it != s->built.end() && before(*it, r))
                 ++it;
         s->built.insert(it, r);
 }
@@ -192,24 +214,43 @@ void dispatcher_main(acdalm_server_t * s)
                         r->t_done = Clock::now();
                         r->state = r->ret < 0 ? FAILED : DONE;
                         s->in_use -= r->footprint;
+                        s->sms_busy -= r->team;
                         s->finished.push_back(r->id);
                         s->completed++;
                         s->cv_done.notify_all();
                 }
-                // admit built requests while memory and slots allow
+                // admit built requests while SMs, memory and slots allow
                 for (;;) {
                         Request * r = nullptr;
                         {
                                 std::lock_guard<std::mutex> g(s->mu);
                                 if (s->built.empty() || (int)s->running.size() >= s->max_inflight)
                                         break;
-                                Request * head = s->built.front();
                                 bool nothing_running = s->running.empty();
-                                if (s->in_use + head->footprint > s->budget && !nothing_running)
+                                auto now = Clock::now();
+                                auto pick = s->built.end();
+                                for (auto it = s->built.begin(); it != s->built.end(); ++it) {
+                                        Request * q = *it;
+                                        bool fits = (nothing_running ||
+                                                     s->sms_busy + q->team <= s->sms) &&
+                                                    (nothing_running ||
+                                                     s->in_use + q->footprint <= s->budget);
+                                        if (fits) {
+                                                pick = it;
+                                                break;
+                                        }
+                                        // a request kept waiting too long
+                                        // blocks the smaller ones behind it
+                                        if (std::chrono::duration<double>(now - q->t_built).count()
+                                            > kBackfillSeconds)
+                                                break;
+                                }
+                                if (pick == s->built.end())
                                         break;
+                                Request * head = *pick;
                                 if (head->footprint > s->budget && nothing_running) {
                                         // can never fit: fail it rather than stall
-                                        s->built.pop_front();
+                                        s->built.erase(pick);
                                         head->state = FAILED;
                                         head->ret = ACDALM_ENOMEM;
                                         head->t_done = Clock::now();
@@ -217,13 +258,15 @@ void dispatcher_main(acdalm_server_t * s)
                                         s->cv_done.notify_all();
                                         continue;
                                 }
-                                s->built.pop_front();
+                                s->built.erase(pick);
                                 s->in_use += head->footprint;
+                                s->sms_busy += head->team;
                                 r = head;
                         }
                         idle = false;
                         approx_t * a = r->alm->approx;
                         alm_t * m = r->alm;
+                        a->dev.priority = r->team > 1 ? s->high_priority : 0;
                         int e = a->dev.create(a->lay);
                         if (!e)
                                 a->dev_ready = true;
@@ -249,6 +292,7 @@ void dispatcher_main(acdalm_server_t * s)
                                 r->ret = e;
                                 r->t_done = Clock::now();
                                 s->in_use -= r->footprint;
+                                s->sms_busy -= r->team;
                                 s->finished.push_back(r->id);
                                 s->cv_done.notify_all();
                         } else {
@@ -273,6 +317,11 @@ extern "C" {
 acdalm_server_t * acdalm_server_create(size_t device_budget, int max_inflight, int precision,
                                        double kkt_tol, int builder_threads)
 {
+        if (precision < 0 || precision > 2) {
+                acd::set_error(ACDALM_EINVAL, "acdalm_server_create: precision mode %d",
+                               precision);
+                return nullptr;
+        }
         if (!acd::device_ready())
                 return nullptr;
         acdalm_server_t * s = new (std::nothrow) acdalm_server;
@@ -285,8 +334,17 @@ acdalm_server_t * acdalm_server_create(size_t device_budget, int max_inflight, i
         }
         s->budget = device_budget;
         s->max_team = acd::max_cluster_team();
+        {
+                int dev = 0;
+                cudaGetDevice(&dev);
+                cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, dev);
+                s->sms = std::max(s->sms, s->max_team);
+        }
         s->max_inflight = max_inflight > 0 ? max_inflight : 128;
         s->precision = precision;
+        int least = 0, greatest = 0;
+        if (cudaDeviceGetStreamPriorityRange(&least, &greatest) == cudaSuccess)
+                s->high_priority = greatest;
         s->kkt_tol = kkt_tol;
         int nb = builder_threads > 0 ? builder_threads
                                      : std::max(1u, std::thread::hardware_concurrency() / 2);
@@ -309,6 +367,7 @@ long long acdalm_server_submit(acdalm_server_t * s, size_t nrows, size_t ncols, 
         auto r = std::make_unique<Request>();
         r->m = nrows;
         r->n = ncols;
+        r->nnz = nnz;
         r->rows.assign(rows, rows + nnz);
         r->cols.assign(cols, cols + nnz);
         r->vals.assign(vals, vals + nnz);

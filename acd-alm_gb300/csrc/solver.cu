@@ -347,7 +347,8 @@ int DevInstance::create(const DeviceLayout & lay)
         log_cap = kLogCap;
         total += rounded((size_t)log_cap * sizeof(LogRec)) + rounded(sizeof(int));
         total += rounded(std::max(sizeof(AlmOut), sizeof(ApproxOut)));
-        ACD_CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), ACDALM_ECUDA);
+        ACD_CUDA_TRY(cudaStreamCreateWithPriority(&stream, cudaStreamNonBlocking, priority),
+                     ACDALM_ECUDA);
         // stream-ordered allocation: no device-wide synchronisation, so a
         // server can admit and retire instances while others run
         cudaError_t e = cudaMallocAsync(&mem, total, stream);
@@ -527,7 +528,7 @@ static int alm_prepare(DevInstance & d, const HostVectors & hv, size_t niter, do
                        double * lam, bool want_log, const AlmSettings & s,
                        const DeviceLayout * lay, AlmKernelArgs & k)
 {
-        bool mixed = s.precision == 1;
+        bool mixed = mixed_for(s.precision, d.nnz);
         if (mixed) {
                 if (!lay) {
                         set_error(ACDALM_EINVAL, "mixed precision needs the device layout");

@@ -22,7 +22,7 @@ _sz = C.c_size_t
 _vp = C.c_void_p
 
 SPMV_SELL, SPMV_BLOCK, SPMV_CSR, SPMV_SELL_FMA = 0, 1, 2, 3
-PRECISION_FP64, PRECISION_MIXED = 0, 1
+PRECISION_FP64, PRECISION_MIXED, PRECISION_AUTO = 0, 1, 2
 
 ERRORS = {-1: "ACDALM_ECUDA", -2: "ACDALM_ETIMEOUT", -3: "ACDALM_ENOMEM",
           -4: "ACDALM_EINVAL", -5: "ACDALM_ENONFINITE", -6: "ACDALM_ENODEV",

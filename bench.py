@@ -148,7 +148,7 @@ def stream_bench(args):
     k = args.stream_count
     arrivals, sizes, seeds = arrivals[:k], sizes[:k], seeds[:k]
     lps = [inst.batch_instance(int(m), int(sd)) for m, sd in zip(sizes, seeds)]
-    prec = 0 if args.precision == "fp64" else 1
+    prec = {"fp64": 0, "mixed": 1, "auto": 2}[args.precision]
     srv = lib.Server(precision=prec, kkt_tol=1e-6)
     t0 = time.perf_counter()
     sub = {}
@@ -467,6 +467,8 @@ def run_reference(args, lp, rank: int):
 
 
 METRIC = "LPs/sec to 1e-6 relative KKT"
+# ACDALM_PRECISION_AUTO runs FP32 inner iterations from this many nonzeros on
+AUTO_MIXED_NNZ = 500_000
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one FP64 inner
 # iteration of the mid LP's solve kernel, from one ncu capture of
@@ -493,7 +495,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--workload", default="mid")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
+    ap.add_argument("--precision", default=None, choices=["fp64", "mixed", "auto"],
                     help="the headline form (fp64: the reference's arithmetic)")
     ap.add_argument("--profile-solve", type=int, default=0,
                     help="run one ALM solve capped at this many inner iterations and exit "
@@ -521,10 +523,17 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=8,
                     help="LPs the plain FP64 comparison solves one at a time")
     args = ap.parse_args()
+    if args.precision is None:
+        # the served stream runs the library's size rule; single LPs the
+        # FP64 drop-in
+        args.precision = "auto" if args.workload == "stream" else "fp64"
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     lp = workload(args.workload)
+    if lp is not None and args.precision == "auto":
+        # ACDALM_PRECISION_AUTO's rule, resolved for this one LP
+        args.precision = "mixed" if lp.nnz >= AUTO_MIXED_NNZ else "fp64"
 
     if args.impl == "reference":
         if rank == 0:
@@ -672,7 +681,8 @@ def main():
                 "d2h_bytes_per_step": 8 * (2 * lp.ncols + 2 * lp.nrows)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                     "traffic_note": TRAFFIC_NOTE,
+                     "traffic_note": TRAFFIC_NOTE if traffic is not None
+                     else "no ncu DRAM capture of this workload",
                      "kernel": "alm_kernel (persistent cooperative solve)",
                      "peak_source": peak_kind,
                      "bytes_per_inner_iteration": {"fp64": bpi, "fp32": bpi32}},

@@ -63,6 +63,11 @@ size_t acdalm_matrix_device_bytes(const struct sparse_matrix * a);
 #define ACDALM_PRECISION_FP64 0  /* everything in FP64 (the default) */
 #define ACDALM_PRECISION_MIXED 1 /* FP32 inner iterations, FP64 outer loop
                                     and final refinement */
+#define ACDALM_PRECISION_AUTO 2  /* MIXED for an LP with at least 500,000
+                                    nonzeros, FP64 below (FP32 iterations
+                                    pay off on large LPs; on small ones
+                                    their extra iterations cost more than
+                                    they save) */
 int alm_set_precision(struct alm *, int mode);
 /* Stop alm_solve when the relative KKT residual (max of the primal, dual
  * and gap terms, FP64, checked after every outer iteration) is <= tol; it

@@ -14,12 +14,16 @@
 // Admission packs the GPU's SMs: every solve holds `team` SMs (one CTA per
 // SM) until it ends, and a request is admitted only while the running
 // teams leave that many SMs free, so no admitted solve waits in the
-// hardware queue holding a slot.  Among built requests the one with the
-// most nonzeros that fits goes first (a large LP started late would set
-// the end of the whole stream); smaller ones fill SMs a larger one cannot
-// use yet, until that one has waited kBackfillSeconds, after which nothing
-// passes it.  Clusters run on high-priority streams: a cluster's CTAs must
-// all find room in one GPC at once.  Every solve is the same computation whether
+// hardware queue holding a slot.  Built requests are taken in this order:
+// one-CTA requests first, in arrival order (they are most requests and
+// little of the work, so running them first cuts the typical latency at
+// almost no cost to the end of the stream), then cluster requests, most
+// nonzeros first (a large LP started late would set the end of the whole
+// stream).  The first request in that order that fits is admitted, so
+// smaller ones fill SMs a larger one cannot use yet -- until a request has
+// waited kBackfillSeconds, after which nothing passes it.  Clusters run on
+// high-priority streams: a cluster's CTAs must all find room in one GPC at
+// once.  Every solve is the same computation whether
 // it runs alone or in the mix (a fixed team, deterministic reductions).
 #include <cuda_runtime.h>
 
@@ -152,9 +156,15 @@ void build_one(acdalm_server_t * s, Request * r)
                                                    acd::mixed_for(s->precision, a->lay.nnz));
         r->state = BUILT;
         r->t_built = Clock::now();
-        // admission order: most nonzeros first, then arrival
+        // admission order: one-CTA requests by arrival, then clusters by
+        // most nonzeros, then arrival
         auto before = [](const Request * p, const Request * q) {
-                return p->nnz != q->nnz ? p->nnz > q->nnz : p->id < q->id;
+                bool ps = p->team == 1, qs = q->team == 1;
+                if (ps != qs)
+                        return ps;
+                if (!ps && p->nnz != q->nnz)
+                        return p->nnz > q->nnz;
+                return p->id < q->id;
         };
         auto it = s->built.begin();
         while (it != s->built.end() && before(*it, r))

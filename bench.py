@@ -198,6 +198,49 @@ def stream_bench(args):
                       "vs_plain_fp64": rate / plain}), flush=True)
 
 
+def cusparse_comparator(lp, reps, flush, peak):
+    """The library comparator for the SpMV kernels: cuSPARSE's CSR product
+    through torch's sparse CSR matmul (one right-hand side), y = A x and
+    y = A'x in FP64 and FP32, with the same L2 flush and byte model."""
+    import scipy.sparse as sp
+    import torch
+    out = []
+    try:
+        a = sp.csr_matrix((lp.vals, (lp.rows, lp.cols)), shape=(lp.nrows, lp.ncols))
+        for t, mat in ((0, a), (1, a.T.tocsr())):
+            for dt in (torch.float64, torch.float32):
+                op = torch.sparse_csr_tensor(
+                    torch.from_numpy(mat.indptr.astype(np.int32)).cuda(),
+                    torch.from_numpy(mat.indices.astype(np.int32)).cuda(),
+                    torch.from_numpy(mat.data).to(dt).cuda(), size=mat.shape)
+                x = torch.rand(mat.shape[1], 1, dtype=dt, device="cuda")
+                for _ in range(3):
+                    y = op @ x
+                stream = torch.cuda.current_stream()
+                times = []
+                for _ in range(reps):
+                    flush.fill_(1.0)
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    y = op @ x
+                    e1.record(stream)
+                    torch.cuda.synchronize()
+                    times.append(e0.elapsed_time(e1) * 1e-3)
+                sec = statistics.median(times)
+                sv = 4 if dt == torch.float32 else 8
+                ny, nx = mat.shape
+                nbytes = lp.nnz * (sv + 4) + 4 * (ny + 1) + sv * (nx + ny)
+                out.append({"variant": "cusparse_csr", "op": "A'x" if t else "Ax",
+                            "dtype": "f32" if sv == 4 else "f64", "us": round(sec * 1e6, 1),
+                            "gbs": round(nbytes / sec / 1e9, 1),
+                            "frac": round(nbytes / sec / 1e9 / peak, 3)})
+                del op, x, y
+    except Exception as e:  # the comparator is reported, never required
+        out.append({"variant": "cusparse_csr", "error": str(e)[:200]})
+    return out
+
+
 def spmv_bench(args, lp):
     """--spmv: y = A x and y = A'x on the device, every layout variant, FP64
     and FP32, L2 flushed before each timed launch; GB/s from the algorithmic
@@ -253,7 +296,8 @@ def spmv_bench(args, lp):
                          "frac": best["gbs"] / peak, "traffic": None,
                          "kernel": f"{best['variant']} {best['op']} {best['dtype']}",
                          "peak_source": peak_kind},
-            "variants": out}
+            "variants": out,
+            "library_comparator": cusparse_comparator(lp, args.spmv_reps, flush, peak)}
     print(json.dumps(line), flush=True)
     m.free()
 
@@ -475,7 +519,7 @@ AUTO_MIXED_NNZ = 500_000
 # `bench.py --profile-solve 3000` (3,000 FP64 iterations;
 # profiles/alm_kernel_mid_traffic.md).  FP32 iterations are scaled by their
 # algorithmic bytes.
-MID_DRAM_BYTES_PER_FP64_ITER = (13897512448 + 5532968192) / 3000
+MID_DRAM_BYTES_PER_FP64_ITER = (27516251648 + 10049832192) / 3000
 TRAFFIC_NOTE = ("ncu DRAM bytes per launch, scaled from a 3,000-iteration capture of the "
                 "same kernel; the instance stays in L2, so traffic is far below the "
                 "algorithmic bytes")
@@ -705,6 +749,10 @@ def main():
         per_lp, source = inner_per_lp_of(args, fallback=mean_inner if not fp32 else None)
         line["cpu_baseline"] = cpu_baseline(lp, per_lp, args.ref_iters,
                                             os.cpu_count() or 1, source)
+        # the same loop on one thread (a shorter sample)
+        one = cpu_baseline(lp, per_lp, max(200, args.ref_iters // 16), 1, source)
+        line["cpu_baseline"]["single_thread"] = {
+            k: one[k] for k in ("value", "cores", "sample", "ms_per_iteration")}
     if rank == 0:
         print(json.dumps(line), flush=True)
     alm.free()

@@ -364,6 +364,17 @@ acdalm_server_t * acdalm_server_create(size_t device_budget, int max_inflight, i
         return s;
 }
 
+int acdalm_server_set_inner_budget(acdalm_server_t * s, uint64_t budget)
+{
+        if (!s) {
+                acd::set_error(ACDALM_EINVAL, "acdalm_server_set_inner_budget: NULL server");
+                return ACDALM_EINVAL;
+        }
+        std::lock_guard<std::mutex> g(s->mu);
+        s->inner_budget = budget;
+        return 0;
+}
+
 long long acdalm_server_submit(acdalm_server_t * s, size_t nrows, size_t ncols, size_t nnz,
                                const uint32_t * rows, const uint32_t * cols,
                                const double * vals, const double * rhs, const double * linear,

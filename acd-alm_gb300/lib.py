@@ -142,6 +142,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.acdalm_server_result.argtypes = [_vp, C.c_longlong, _vp, _vp, C.POINTER(Stats),
                                        C.POINTER(C.c_double)]
     L.acdalm_server_destroy.argtypes = [_vp]
+    L.acdalm_server_set_inner_budget.argtypes = [_vp, C.c_uint64]
     L.thread_pool_init.restype = _vp
     L.thread_pool_init.argtypes = [C.c_uint]
     L.thread_pool_free.argtypes = [_vp]
@@ -500,6 +501,10 @@ class Server:
         r = lib().acdalm_server_result(self.h, rid, x.ctypes.data_as(_vp),
                                        lam.ctypes.data_as(_vp), C.byref(st), C.byref(lat))
         return r, x, lam, st.as_dict(), lat.value
+
+    def set_inner_budget(self, budget: int):
+        check(lib().acdalm_server_set_inner_budget(self.h, budget),
+              "acdalm_server_set_inner_budget")
 
     def close(self):
         if self.h:

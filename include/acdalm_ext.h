@@ -147,14 +147,17 @@ int acdalm_batch_free(acdalm_batch_t * b);
 /* A server accepts LPs at any time and solves them to a relative KKT
  * residual <= kkt_tol (alm_solve with alm_set_kkt_tolerance; precision an
  * ACDALM_PRECISION_* mode).  Builder threads (builder_threads, 0 = half
- * the cores) prepare each LP's layouts in arrival order; requests are
- * admitted, in arrival order, while their device footprint fits
+ * the cores) prepare each LP's layouts in arrival order.  Each LP runs in
+ * its own launch and stream, beside the others: on one CTA up to 150,000
+ * nonzeros, on a thread-block cluster of 4, 8 or 16 CTAs above that, one
+ * CTA per SM.  Built requests are admitted while the running solves leave
+ * enough SMs free for the request's team, its device footprint fits
  * device_budget bytes (0 = 80% of the free memory) and fewer than
- * max_inflight solves run (0 = 128).  Each admitted LP runs in its own
- * launch and stream, beside the others: on one CTA up to 150,000 nonzeros,
- * on a thread-block cluster of 4, 8 or 16 CTAs above that; a finished solve
- * is retired and its memory returned.  The result of an LP does not depend
- * on what else runs (a fixed team, deterministic reductions). */
+ * max_inflight solves run (0 = 128): one-CTA requests first in arrival
+ * order, then cluster requests with the most nonzeros first; a request
+ * passed over for 10 s blocks the ones behind it.  A finished solve is
+ * retired and its memory returned.  The result of an LP does not depend on
+ * what else runs (a fixed team, deterministic reductions). */
 typedef struct acdalm_server acdalm_server_t;
 acdalm_server_t * acdalm_server_create(size_t device_budget, int max_inflight,
                                        int precision, double kkt_tol,
@@ -181,6 +184,9 @@ int acdalm_server_result(acdalm_server_t * s, long long id, double * x,
 /* Stops the server after the running solves finish; unfinished requests
  * are dropped. */
 int acdalm_server_destroy(acdalm_server_t * s);
+/* Caps each request built after the call at `budget` inner iterations in
+ * all (alm_set_inner_budget); 0 = no cap, the default. */
+int acdalm_server_set_inner_budget(acdalm_server_t * s, uint64_t budget);
 
 /* ---- layout inspection (for parity checks against the reference) ---- */
 /* The 4-row block arena of A (transpose = 0) or A' (1), byte for byte the

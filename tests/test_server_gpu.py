@@ -121,3 +121,26 @@ def test_large_lp_cluster_mixed_precision(instances, oracle_lib):
     assert x.tobytes() == again[1].tobytes()
     obj = _oracle_objective(oracle_lib, instances, lp, threads=8)
     assert abs(k["objective"] - obj) <= 1e-5 * (abs(obj) + 1), (k, obj)
+
+
+def test_server_inner_budget_caps_each_request(instances):
+    """acdalm_server_set_inner_budget caps every request built after it:
+    a one-CTA LP and a cluster LP each stop at the cap (alm_solve's 1, the
+    iteration limit) instead of solving to the tolerance."""
+    b = binding()
+    small = instances.batch_instance(400, 91)
+    large = instances.batch_instance(20000, 92)  # 240k nonzeros: a cluster
+    srv = b.Server(precision=0, kkt_tol=1e-6)
+    srv.set_inner_budget(150)
+    ids = [srv.submit(small), srv.submit(large)]
+    out = {}
+    deadline = time.time() + 120
+    while len(out) < 2 and time.time() < deadline:
+        for rid in srv.poll(timeout=0.5):
+            out[rid] = srv.result(rid)
+    srv.close()
+    assert len(out) == 2
+    for rid in ids:
+        r, x, lam, st, lat = out[rid]
+        assert r == 1, (r, st)
+        assert 0 < st["inner_iterations"] <= 150, st

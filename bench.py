@@ -241,6 +241,27 @@ def cusparse_comparator(lp, reps, flush, peak):
     return out
 
 
+def served_probe(args):
+    """--served M --profile-solve N: one LP of the served-stream family
+    (m = M, n = 2m, 6 nonzeros per column) alone in a server, capped at N
+    inner iterations (the command the ncu captures of the one-CTA and
+    cluster kernels use)."""
+    lib = importlib.import_module("acd-alm_gb300.lib")
+    lp = inst.batch_instance(args.served, 12345 + args.served)
+    prec = {"fp64": 0, "mixed": 1, "auto": 2}[args.precision]
+    srv = lib.Server(precision=prec, kkt_tol=1e-6)
+    srv.set_inner_budget(args.profile_solve)
+    srv.submit(lp)
+    got = []
+    while not got:
+        got = srv.poll(timeout=1.0)
+    r, x, lam, st, lat = srv.result(got[0])
+    srv.close()
+    print(json.dumps({"served": args.served, "nnz": lp.nnz, "precision": args.precision,
+                      "profile_solve": args.profile_solve, "ret": r,
+                      "inner": st["inner_iterations"], "device_seconds": st["seconds"]}))
+
+
 def spmv_bench(args, lp):
     """--spmv: y = A x and y = A'x on the device, every layout variant, FP64
     and FP32, L2 flushed before each timed launch; GB/s from the algorithmic
@@ -544,6 +565,10 @@ def main():
     ap.add_argument("--profile-solve", type=int, default=0,
                     help="run one ALM solve capped at this many inner iterations and exit "
                          "(the command the ncu captures use)")
+    ap.add_argument("--served", type=int, default=0,
+                    help="with --profile-solve: serve one LP of the served-stream family "
+                         "with this many rows instead (one CTA or a cluster, as the server "
+                         "picks), capped the same way")
     ap.add_argument("--trace", type=int, default=0,
                     help="trace this many grid-team reductions (from the 2,001st) of one "
                          "solve capped at 3,000 inner iterations; print the phase breakdown")
@@ -571,6 +596,9 @@ def main():
         # the served stream runs the library's size rule; single LPs the
         # FP64 drop-in
         args.precision = "auto" if args.workload == "stream" else "fp64"
+    if args.served and args.profile_solve:
+        served_probe(args)
+        return
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

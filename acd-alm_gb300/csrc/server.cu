@@ -11,19 +11,13 @@
 // solves are retired (results read back, device memory freed), which frees
 // budget for the next requests.
 //
-// Admission packs the GPU's SMs: every solve holds `team` SMs (one CTA per
-// SM) until it ends, and a request is admitted only while the running
-// teams leave that many SMs free, so no admitted solve waits in the
-// hardware queue holding a slot.  Built requests are taken in this order:
-// one-CTA requests first, in arrival order (they are most requests and
-// little of the work, so running them first cuts the typical latency at
-// almost no cost to the end of the stream), then cluster requests, most
-// nonzeros first (a large LP started late would set the end of the whole
-// stream).  The first request in that order that fits is admitted, so
-// smaller ones fill SMs a larger one cannot use yet -- until a request has
-// waited kBackfillSeconds, after which nothing passes it.  Clusters run on
-// high-priority streams: a cluster's CTAs must all find room in one GPC at
-// once.  Every solve is the same computation whether
+// Admission packs the GPU's SMs (admission.h): a request is admitted only
+// while the running teams leave enough SMs free for its team, so no
+// admitted solve waits in the hardware queue holding a slot; one-CTA
+// requests go first, then clusters with the most nonzeros, and smaller
+// requests fill SMs a larger one cannot use yet until it has waited
+// kBackfillSeconds.  Clusters run on high-priority streams: a cluster's
+// CTAs must all find room in one GPC at once.  Every solve is the same computation whether
 // it runs alone or in the mix (a fixed team, deterministic reductions).
 #include <cuda_runtime.h>
 
@@ -40,6 +34,7 @@
 
 #include "../../include/acdalm_ext.h"
 #include "../../include/alm.h"
+#include "admission.h"
 #include "common.h"
 #include "instance.h"
 #include "layout.h"
@@ -109,6 +104,18 @@ struct acdalm_server {
 
 namespace {
 
+// A built request as the admission rule sees it at time `now`.
+acd::Candidate candidate(const Request * r, Clock::time_point now)
+{
+        acd::Candidate c;
+        c.id = r->id;
+        c.nnz = r->nnz;
+        c.team = r->team;
+        c.footprint = r->footprint;
+        c.waited = std::chrono::duration<double>(now - r->t_built).count();
+        return c;
+}
+
 // Cluster size (CTAs per LP) for an LP with nnz nonzeros.
 int team_size(long long nnz)
 {
@@ -156,18 +163,10 @@ void build_one(acdalm_server_t * s, Request * r)
                                                    acd::mixed_for(s->precision, a->lay.nnz));
         r->state = BUILT;
         r->t_built = Clock::now();
-        // admission order: one-CTA requests by arrival, then clusters by
-        // most nonzeros, then arrival
-        auto before = [](const Request * p, const Request * q) {
-                bool ps = p->team == 1, qs = q->team == 1;
-                if (ps != qs)
-                        return ps;
-                if (!ps && p->nnz != q->nnz)
-                        return p->nnz > q->nnz;
-                return p->id < q->id;
-        };
+        // keep the built queue in admission order
         auto it = s->built.begin();
-        while (it != s->built.end() && before(*it, r))
+        while (it != s->built.end() && acd::admits_before(candidate(*it, r->t_built),
+                                                          candidate(r, r->t_built)))
                 ++it;
         s->built.insert(it, r);
 }
@@ -238,25 +237,19 @@ void dispatcher_main(acdalm_server_t * s)
                                         break;
                                 bool nothing_running = s->running.empty();
                                 auto now = Clock::now();
-                                auto pick = s->built.end();
-                                for (auto it = s->built.begin(); it != s->built.end(); ++it) {
-                                        Request * q = *it;
-                                        bool fits = (nothing_running ||
-                                                     s->sms_busy + q->team <= s->sms) &&
-                                                    (nothing_running ||
-                                                     s->in_use + q->footprint <= s->budget);
-                                        if (fits) {
-                                                pick = it;
-                                                break;
-                                        }
-                                        // a request kept waiting too long
-                                        // blocks the smaller ones behind it
-                                        if (std::chrono::duration<double>(now - q->t_built).count()
-                                            > kBackfillSeconds)
-                                                break;
-                                }
-                                if (pick == s->built.end())
+                                acd::Capacity cap;
+                                cap.sms = s->sms;
+                                cap.sms_busy = s->sms_busy;
+                                cap.budget = s->budget;
+                                cap.in_use = s->in_use;
+                                cap.nothing_running = nothing_running;
+                                cap.backfill_seconds = kBackfillSeconds;
+                                long at = acd::pick_admission(
+                                        s->built.size(),
+                                        [&](size_t i) { return candidate(s->built[i], now); }, cap);
+                                if (at < 0)
                                         break;
+                                auto pick = s->built.begin() + at;
                                 Request * head = *pick;
                                 if (head->footprint > s->budget && nothing_running) {
                                         // can never fit: fail it rather than stall

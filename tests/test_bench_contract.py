@@ -58,3 +58,13 @@ def test_reference_arm_line_fits_its_own_run(monkeypatch, capsys, instances):
     assert abs(line["value"] * p["ms_per_iteration"] * 1e-3 * p["inner_iterations_per_lp"]
                - 1.0) < 0.5
     assert line["e2e"]["value"] == line["value"]
+
+
+def test_auto_precision_threshold_matches_the_library():
+    """bench.py resolves --precision auto with the library's own rule
+    (mixed_for in csrc/instance.h): the two thresholds must agree."""
+    import re
+    b = _bench()
+    text = open(os.path.join(ROOT, "acd-alm_gb300", "csrc", "instance.h")).read()
+    lib_nnz = int(re.search(r"kAutoMixedNnz\s*=\s*(\d+)", text).group(1))
+    assert b.AUTO_MIXED_NNZ == lib_nnz

@@ -303,7 +303,7 @@ struct TeamCtl {
 // (a naturally aligned 64-bit store is seen whole or not at all).
 constexpr int kSlotStride = 16;  // words per line
 // Lines a lane polls at once, per pass over the CTAs: 10 covers 320 CTAs
-// (2 per SM) in one pass; more CTAs take further passes.
+// (two per SM on 152 SMs) in one pass; more CTAs take further passes.
 constexpr int kSumWidth = 10;
 __device__ __forceinline__ ulonglong2 ld_relaxed_u64x2(const unsigned long long * p)
 {

@@ -15,7 +15,7 @@
 
 namespace acd {
 
-constexpr int kThreads = 256;       // grid-team CTAs (2 per SM)
+constexpr int kThreads = 512;       // grid-team CTAs (1 per SM)
 constexpr int kBatchThreads = 512;  // one-CTA and cluster teams: 16 warps of memory parallelism
 
 struct AlmKernelArgs {
@@ -35,7 +35,7 @@ struct AlmKernelArgs {
 // Trace: the grid team records phase timestamps (a separate instantiation,
 // so the untraced solve pays nothing for it).
 template <bool Exact, bool Trace = false>
-__global__ void __launch_bounds__(kThreads, 2) alm_kernel(AlmKernelArgs k)
+__global__ void __launch_bounds__(kThreads, 1) alm_kernel(AlmKernelArgs k)
 {
         GridTeamT<Trace> tm{k.ctl, k.slots, k.result, 0, 0u};
         Alm<GridTeamT<Trace>, Exact> alm(tm, k.P, k.W, k.log, k.M);
@@ -68,7 +68,7 @@ struct ApproxKernelArgs {
 };
 
 template <bool Exact>
-__global__ void __launch_bounds__(kThreads, 2) approx_kernel(ApproxKernelArgs k)
+__global__ void __launch_bounds__(kThreads, 1) approx_kernel(ApproxKernelArgs k)
 {
         GridTeam tm{k.ctl, k.slots, k.result, 0, 0u};
         Approx<double, GridTeam, Exact> ap(tm, k.P, k.W, k.log);
@@ -208,7 +208,7 @@ struct Spg {
 };
 
 template <bool Exact>
-__global__ void __launch_bounds__(kThreads, 2) mpg_kernel(ApproxKernelArgs k)
+__global__ void __launch_bounds__(kThreads, 1) mpg_kernel(ApproxKernelArgs k)
 {
         GridTeam tm{k.ctl, k.slots, k.result, 0, 0u};
         Approx<double, GridTeam, Exact> ap(tm, k.P, k.W, k.log);

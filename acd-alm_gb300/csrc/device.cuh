@@ -8,10 +8,10 @@
 // the barrier between phases.
 //
 //   GridTeam    - every CTA of a cooperative launch (one large LP).  Each
-//                 CTA publishes its partials in its own line with a
-//                 release-stored epoch tag; every CTA waits for all tags and
-//                 sums all lines itself in CTA order, so every CTA reads the
-//                 same bits.
+//                 CTA publishes its partials in its own line, every word
+//                 tagged with the reduction's epoch; every CTA polls all
+//                 lines until the tags match and sums them itself in CTA
+//                 order, so every CTA reads the same bits.
 //   BlockTeam   - one CTA (one small LP of a batch); __syncthreads based.
 //   ClusterTeam - the CTAs of one thread-block cluster (a large served LP);
 //                 partials read through distributed shared memory, hardware

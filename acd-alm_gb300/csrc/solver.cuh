@@ -213,7 +213,13 @@ struct Approx {
                 const T ts = T(1) - th, tt = th, ns = T(1) - nth, nt = nth;
                 constexpr int S = kViolStride;
                 // with the momentum update, v is zp: the next y's violation
-                // goes to the second half of v's pair, beside v's own
+                // goes to the second half of v's pair, beside v's own, in
+                // one pair-sized store (v.viol must start a pair)
+                if (linterp &&
+                    (reinterpret_cast<uintptr_t>(v.viol) & (S * sizeof(T) - 1)) != 0) {
+                        tm.fail(kStatusInternal);
+                        return false;
+                }
                 T * xvw = (linterp == 2) ? W.alt_xv : x.viol;
                 T * xxw = (linterp == 2) ? W.alt_x : x.x;
                 const T * xvr = x.viol;

@@ -17,8 +17,9 @@
 // requests go first, then clusters with the most nonzeros, and smaller
 // requests fill SMs a larger one cannot use yet until it has waited
 // kBackfillSeconds.  Clusters run on high-priority streams: a cluster's
-// CTAs must all find room in one GPC at once.  Every solve is the same computation whether
-// it runs alone or in the mix (a fixed team, deterministic reductions).
+// CTAs must all find room in one GPC at once.  Every solve is the same
+// computation whether it runs alone or in the mix (a fixed team,
+// deterministic reductions).
 #include <cuda_runtime.h>
 
 #include <atomic>

@@ -2,18 +2,19 @@
 //
 // Requests (an LP each) are submitted at any time.  A pool of builder
 // threads turns each into its host layouts (the permuted copy and the
-// device layout) in arrival order.  A dispatcher thread admits built
-// requests while their device footprint fits the memory budget and fewer
-// than max_inflight solves run: each admitted LP gets its device instance,
-// its data uploaded, and one solve launched on its own stream -- one CTA for
-// a small LP, a thread-block cluster of up to 16 CTAs for a large one -- so
-// LPs that arrive while others are on the GPU run beside them.  Finished
-// solves are retired (results read back, device memory freed), which frees
+// device layout), one-CTA requests before larger ones (a larger one that
+// has waited kBackfillSeconds goes next).  A dispatcher thread admits built
+// requests: each admitted LP gets its device instance, its data uploaded,
+// and one solve launched on its own stream -- one CTA for a small LP, a
+// thread-block cluster of up to 16 CTAs for a large one -- so LPs that
+// arrive while others are on the GPU run beside them.  Finished solves are
+// retired (results read back, device memory freed), which frees SMs and
 // budget for the next requests.
 //
 // Admission packs the GPU's SMs (admission.h): a request is admitted only
-// while the running teams leave enough SMs free for its team, so no
-// admitted solve waits in the hardware queue holding a slot; one-CTA
+// while the running teams leave enough SMs free for its team, its device
+// footprint fits the memory budget and fewer than max_inflight solves run,
+// so no admitted solve waits in the hardware queue holding a slot; one-CTA
 // requests go first, then clusters with the most nonzeros, and smaller
 // requests fill SMs a larger one cannot use yet until it has waited
 // kBackfillSeconds.  Clusters run on high-priority streams: a cluster's
@@ -91,7 +92,8 @@ struct acdalm_server {
         std::mutex mu;
         std::condition_variable cv_build, cv_done;
         std::map<long long, std::unique_ptr<Request>> reqs;
-        std::deque<Request *> to_build;  // submitted, not built
+        // submitted, not built: LPs a single CTA solves, and the rest
+        std::deque<Request *> to_build_small, to_build_large;
         std::deque<Request *> built;     // built, not admitted (arrival order)
         std::vector<Request *> running;
         std::deque<long long> finished;  // retired, not yet polled
@@ -178,11 +180,23 @@ void builder_main(acdalm_server_t * s)
                 Request * r;
                 {
                         std::unique_lock<std::mutex> g(s->mu);
-                        s->cv_build.wait(g, [&] { return s->stop || !s->to_build.empty(); });
+                        s->cv_build.wait(g, [&] {
+                                return s->stop || !s->to_build_small.empty() ||
+                                       !s->to_build_large.empty();
+                        });
                         if (s->stop)
                                 return;
-                        r = s->to_build.front();
-                        s->to_build.pop_front();
+                        // one-CTA requests first (they are admitted first,
+                        // and their builds are short), unless a larger one
+                        // has waited longer than the backfill limit
+                        bool large = !s->to_build_large.empty() &&
+                                     (s->to_build_small.empty() ||
+                                      std::chrono::duration<double>(
+                                              Clock::now() - s->to_build_large.front()->t_submit)
+                                                      .count() > kBackfillSeconds);
+                        std::deque<Request *> & q = large ? s->to_build_large : s->to_build_small;
+                        r = q.front();
+                        q.pop_front();
                 }
                 build_one(s, r);
         }
@@ -402,7 +416,8 @@ long long acdalm_server_submit(acdalm_server_t * s, size_t nrows, size_t ncols, 
         std::lock_guard<std::mutex> g(s->mu);
         long long id = s->next_id++;
         r->id = id;
-        s->to_build.push_back(r.get());
+        (team_size((long long)nnz) == 1 ? s->to_build_small : s->to_build_large)
+                .push_back(r.get());
         s->reqs[id] = std::move(r);
         s->cv_build.notify_one();
         return id;

@@ -147,7 +147,8 @@ int acdalm_batch_free(acdalm_batch_t * b);
 /* A server accepts LPs at any time and solves them to a relative KKT
  * residual <= kkt_tol (alm_solve with alm_set_kkt_tolerance; precision an
  * ACDALM_PRECISION_* mode).  Builder threads (builder_threads, 0 = half
- * the cores) prepare each LP's layouts in arrival order.  Each LP runs in
+ * the cores) prepare each LP's layouts, one-CTA requests first (a larger
+ * one that has waited 10 s goes next).  Each LP runs in
  * its own launch and stream, beside the others: on one CTA up to 150,000
  * nonzeros, on a thread-block cluster of 4, 8 or 16 CTAs above that, one
  * CTA per SM.  Built requests are admitted while the running solves leave
